@@ -1,0 +1,290 @@
+"""Benchmark of the mole walker hot path on GB300.
+
+Workload (default): the H2 Slater-Pade VMC + SR optimisation at its full size
+-- nuclei at z = +-0.7 bohr, psi = sigma(r1) sigma(r2) exp(r12 / (2 (1 + b r12))),
+65,536 walkers, single-electron Gaussian moves of 0.4 bohr, 2,000 sweeps per SR
+iteration with the local energy and the O_k, E O_k, O_k O_l sums on every
+sweep, then the FP64 SR solve (eps 1e-3, step 0.05) and the parameter update.
+One bench step is one SR iteration. Metric: walker-steps/s including E_L.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the reference's CPU call pattern (the C++ restatement
+in oracle/faithful.cpp) on all host cores for the same workload, one bounded
+sample of walkers per step. Under torchrun every rank runs an independent
+replica (the path shards by walkers with no data-path exchange) and the value
+is the sum over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "walker-steps/s incl. E_L"
+WORKLOAD = "H2 Slater-Pade VMC + SR, 65536 walkers, Gaussian moves 0.4 bohr, 2000 sweeps per SR iteration"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--walkers", type=int, default=65536)
+    p.add_argument("--sweeps", type=int, default=2000)
+    p.add_argument("--block", type=int, default=100)
+    p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    p.add_argument("--no-extras", action="store_true", help="skip the e2e, mixed and CPU-baseline legs")
+    return p.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self) -> dict:
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread is not None:
+            self.thread.join(timeout=5)
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows if len(r) >= 9 for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(sm)}
+
+
+def cpu_baseline_sample(threads: int, walkers: int, sweeps: int):
+    """The reference's call pattern (oracle/faithful.cpp) on the same workload."""
+    from oracle import oracle as O
+
+    O.build()
+    secs, e = O.faithful_vmc(1, walkers, 0, sweeps, 1, 0.4, 1.0, 0.5, True, threads, 1)
+    return walkers * sweeps / secs, secs, e
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+
+    O.build()
+    threads = O.hardware_threads()
+    walkers, sweeps = 256 * threads, 1000
+    for _ in range(args.warmup):
+        cpu_baseline_sample(threads, walkers, 20)
+    rates, secs = [], 0.0
+    for _ in range(args.steps):
+        r, s, _ = cpu_baseline_sample(threads, walkers, sweeps)
+        rates.append(r)
+        secs += s
+    value = args.steps * walkers * sweeps / secs
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "walker-steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "walkers_per_step_sample": walkers, "sweeps_per_step_sample": sweeps},
+            "cpu_baseline": {"value": value, "unit": "walker-steps/s", "cores": threads, "kind": "port",
+                             "sample": f"{walkers} walkers x {sweeps} sweeps per step, reference call pattern "
+                                       "(oracle/faithful.cpp), std::thread over all host cores"},
+            "e2e": {"value": value, "unit": "walker-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+
+    from mole_gb300 import api, flop_model
+    from mole_gb300 import system as S
+    from mole_gb300.system import MOVE_GAUSS
+
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+    prec = api.PREC_MIXED if args.precision == "mixed" else api.PREC_FP64
+
+    ctx = api.Context(local)
+    ctx.set_stream(stream.cuda_stream)
+    W, sweeps, block = args.walkers, args.sweeps, args.block
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    def make(precision):
+        wf = api.WaveFunction(ctx, S.h2(1.0, 0.5))
+        wk = api.Walkers(wf, W, seed=0x5EED + 1 + rank)
+        sampler = api.Sampler(wf, api.MetropolisGaussian(0.4), wk, precision=precision)
+        sampler.run(200, 0, 1)  # equilibrate (untimed)
+        return wf, wk, sampler
+
+    sr = api.StochasticReconfiguration(0.05, 1e-3)
+
+    def sr_step(wf, sampler):
+        r = sampler.run(0, sweeps, block, sr=True)
+        wf.update_parameters(sr.compute_parameter_update(wf.parameters(), r, ctx))
+        return r
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def timed(fn, steps):
+        barrier()
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(steps):
+            flush.zero_()  # evict L2 between iterations
+            fn()
+        t1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        ms = t0.elapsed_time(t1)
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    # ------------------------------------------------------------ device leg
+    wf, wk, sampler = make(prec)
+    results = []
+    for _ in range(args.warmup):
+        sr_step(wf, sampler)
+    ctx.enable_timing(True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms = timed(lambda: results.append(sr_step(wf, sampler)), args.steps)
+    clk = clocks.stop()
+    k_ms, k_n = ctx.kernel_time(0)
+    ctx.enable_timing(False)
+    ws_per_step = W * sweeps
+    value = world * args.steps * ws_per_step / (ms * 1e-3)
+    last = results[-1]
+    acc = last.acceptance
+
+    fp64_peak, fp32_peak = ctx.probe_peaks()
+    work = flop_model.walker_step(S.h2(), MOVE_GAUSS, 2, acc)
+    per_launch = work.flops * ws_per_step
+    achieved = per_launch / (k_ms / k_n * 1e-3) / 1e12
+    peak = (fp64_peak if prec == api.PREC_FP64 else fp32_peak) / 1e3
+    roofline = {"bound": "fp64" if prec == api.PREC_FP64 else "fp32", "achieved": achieved, "peak": peak,
+                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                "kernel": "vmc_kernel<1,1,double,2,false>" if prec == api.PREC_FP64 else "vmc_kernel<1,1,float,2,false>",
+                "kernel_ms_per_launch": k_ms / k_n, "flops_per_walker_step": work.flops,
+                "special_per_walker_step": work.special,
+                "peak_source": "measured live: FMA-chain probe (mole_probe_peaks)"}
+
+    line = {"metric": METRIC, "value": value, "unit": "walker-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if prec == api.PREC_FP64 else "f32/f64-mixed", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "walkers_per_gpu": W, "sweeps_per_step": sweeps, "block_size": block,
+                       "sr_params": 2, "precision": args.precision, "parallelism": f"replicas x{world}",
+                       "l2": "flushed between steps (256 MiB write); walker state 3 MiB"},
+            "gpu_launches": args.steps * 3,
+            "energy": last.energy, "energy_error": last.error, "acceptance": acc,
+            "params": [float(x) for x in wf.parameters()],
+            "roofline": roofline, "clocks": clk,
+            "peaks_measured": {"fp64_gflops": fp64_peak, "fp32_gflops": fp32_peak}}
+
+    if not args.no_extras:
+        # -------------------------------------------------- e2e through the C ABI
+        N = 2
+        host_in = torch.empty((W, N, 3), dtype=torch.float64, pin_memory=True)
+        host_out = torch.empty((W, N, 3), dtype=torch.float64, pin_memory=True)
+        host_in.copy_(torch.from_numpy(wk.positions()))
+        hin, hout = host_in.numpy(), host_out.numpy()
+        k2 = max(3, args.steps // 2)
+
+        def e2e_step():
+            wk.set_positions(hin)
+            sr_step(wf, sampler)
+            wk.wf.lib.mole_walkers_get_positions(wk.h, api.dptr(hout), hout.size)
+
+        e2e_step()
+        e_ms = timed(e2e_step, k2)
+        line["e2e"] = {"value": world * k2 * ws_per_step / (e_ms * 1e-3), "unit": "walker-steps/s",
+                       "h2d_bytes_per_step": int(hin.nbytes), "d2h_bytes_per_step": int(hout.nbytes + 8 * (7 + 2 + 2 + 4))}
+        # -------------------------------------------------- mixed-precision form
+        if prec == api.PREC_FP64:
+            wf2, wk2, s2 = make(api.PREC_MIXED)
+            wf2.set_parameters(wf.parameters())
+            for _ in range(2):
+                s2.run(0, sweeps, block, sr=True)
+            res2 = []
+            m_ms = timed(lambda: res2.append(s2.run(0, sweeps, block, sr=True)), args.steps)
+            r_fp64 = sampler.run(0, sweeps, block, sr=False)
+            line["mixed"] = {"value": world * args.steps * ws_per_step / (m_ms * 1e-3), "unit": "walker-steps/s",
+                             "energy": res2[-1].energy, "energy_error": res2[-1].error,
+                             "energy_fp64_same_params": r_fp64.energy, "energy_fp64_error": r_fp64.error,
+                             "energy_delta_vs_fp64": res2[-1].energy - r_fp64.energy}
+        # -------------------------------------------------- CPU baseline
+        if rank == 0 and world == 1:
+            from oracle import oracle as O
+
+            threads = O.hardware_threads()
+            rate, secs, _ = cpu_baseline_sample(threads, 256 * threads, 1000)
+            line["cpu_baseline"] = {"value": rate, "unit": "walker-steps/s", "cores": threads, "kind": "port",
+                                    "sample": f"{256 * threads} walkers x 1000 sweeps ({secs:.1f} s), reference call "
+                                              "pattern (oracle/faithful.cpp), std::thread over all host cores"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

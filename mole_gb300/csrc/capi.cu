@@ -1,0 +1,799 @@
+// capi.cu -- implementation of the C ABI declared in include/mole_gpu.h.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mole_gpu.h"
+#include "dispatch.cuh"
+#include "ensemble.cuh"
+
+namespace mole {
+#define MOLE_DECL(NU, ND)                           \
+  const KernelSetT<double>* kernels_f64_##NU##_##ND(); \
+  const KernelSetT<float>* kernels_f32_##NU##_##ND();
+MOLE_DECL(1, 0)
+MOLE_DECL(1, 1)
+MOLE_DECL(2, 1)
+MOLE_DECL(2, 2)
+
+#define MOLE_CASE(NU, ND, TAG) \
+  if (nu == NU && nd == ND) return kernels_##TAG##_##NU##_##ND();
+const KernelSetT<double>* kernel_set64(int nu, int nd) {
+  MOLE_CASE(1, 0, f64) MOLE_CASE(1, 1, f64) MOLE_CASE(2, 1, f64) MOLE_CASE(2, 2, f64)
+  return nullptr;
+}
+const KernelSetT<float>* kernel_set32(int nu, int nd) {
+  MOLE_CASE(1, 0, f32) MOLE_CASE(1, 1, f32) MOLE_CASE(2, 1, f32) MOLE_CASE(2, 2, f32)
+  return nullptr;
+}
+}  // namespace mole
+
+using namespace mole;
+
+namespace {
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CUDA_TRY(x)                                                                        \
+  do {                                                                                     \
+    cudaError_t e_ = (x);                                                                  \
+    if (e_ != cudaSuccess) return fail(MOLE_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+// Device buffer grown on demand (the context owns device memory).
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t reserve(size_t m) {
+    if (m <= n) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMalloc(&p, std::max<size_t>(m, 1) * sizeof(T));
+    if (e == cudaSuccess) n = m;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+}  // namespace
+
+struct mole_ctx {
+  int device = 0;
+  int n_sm = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t stream = nullptr;
+  bool timing = false;
+  double kernel_ms[3] = {0, 0, 0};
+  int64_t kernel_launches[3] = {0, 0, 0};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  DevBuf<double> partials, tb_partials, reduced, scratch;
+  DevBuf<int> status;
+};
+
+struct mole_system {
+  mole_ctx* ctx = nullptr;
+  int n_nuc = 0, n_up = 0, n_dn = 0, n_basis = 0, n_exp = 0;
+  std::vector<double> nuc_pos, en_coef, coef_up, coef_dn;
+  std::vector<int> nuc_z, b_center, b_kind, b_exp;
+  int ee_on = 0, ee_npoly = 0, en_on = 0, nn_on = 0, pot_kind = 0;
+  double ee_kappa = 0, cusp_anti = 0.5, cusp_para = 0.25, omega = 0;
+  int P = 0;
+  std::vector<double> theta;
+  SysParams<double> sp64;
+  SysParams<float> sp32;
+  const KernelSetT<double>* k64 = nullptr;
+  const KernelSetT<float>* k32 = nullptr;
+};
+
+struct mole_walkers {
+  mole_system* sys = nullptr;
+  int W = 0;
+  uint64_t seed = 0;
+  uint64_t step = 0;
+  double* pos = nullptr;  // SoA [3N][W]
+  // DMC state (allocated on first DMC call)
+  double *pos2 = nullptr, *eloc = nullptr, *eloc2 = nullptr, *weight = nullptr, *cum = nullptr, *btot = nullptr;
+  double *e_ref = nullptr, *energies = nullptr;
+  size_t energies_n = 0;
+  uint64_t* dstep = nullptr;
+  CombState* comb = nullptr;
+  bool eloc_valid = false;
+};
+
+namespace {
+
+template <class R>
+void fill_params(const mole_system& s, SysParams<R>& sp) {
+  std::memset(&sp, 0, sizeof(sp));
+  sp.n_nuc = s.n_nuc;
+  sp.n_basis = s.n_basis;
+  // basis functions ordered by centre so each nucleus owns a contiguous range
+  std::vector<int> order(s.n_basis);
+  for (int b = 0; b < s.n_basis; ++b) order[b] = b;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return s.b_center[a] < s.b_center[b]; });
+  int pos = 0;
+  for (int I = 0; I < s.n_nuc; ++I) {
+    sp.nuc_b0[I] = pos;
+    while (pos < s.n_basis && s.b_center[order[pos]] == I) ++pos;
+  }
+  sp.nuc_b0[s.n_nuc] = pos;
+  for (int I = 0; I < s.n_nuc; ++I) {
+    for (int c = 0; c < 3; ++c) sp.nuc_pos[3 * I + c] = (R)s.nuc_pos[3 * I + c];
+    sp.nuc_z[I] = (R)s.nuc_z[I];
+    sp.en_coef[I] = (R)s.en_coef[I];
+  }
+  for (int j = 0; j < s.n_basis; ++j) {
+    const int b = order[j];
+    sp.b_kind[j] = s.b_kind[b];
+    sp.b_exp[j] = s.b_exp[b];
+    sp.b_zeta[j] = (R)s.theta[s.b_exp[b]];
+    for (int k = 0; k < s.n_up; ++k) sp.coef[0][k][j] = (R)s.coef_up[(size_t)k * s.n_basis + b];
+    for (int k = 0; k < s.n_dn; ++k) sp.coef[1][k][j] = (R)s.coef_dn[(size_t)k * s.n_basis + b];
+  }
+  sp.n_exp = s.n_exp;
+  sp.off_ee = s.n_exp;
+  sp.off_en = sp.off_ee + (s.ee_on ? 1 + s.ee_npoly : 0);
+  sp.off_nn = sp.off_en + (s.en_on ? 1 : 0);
+  sp.P = s.P;
+  sp.ee_on = s.ee_on;
+  sp.ee_npoly = s.ee_npoly;
+  sp.ee_kappa = (R)s.ee_kappa;
+  sp.cusp_anti = (R)s.cusp_anti;
+  sp.cusp_para = (R)s.cusp_para;
+  if (s.ee_on) {
+    sp.ee_b = (R)s.theta[sp.off_ee];
+    for (int p = 0; p < s.ee_npoly; ++p) sp.ee_poly[p] = (R)s.theta[sp.off_ee + 1 + p];
+  }
+  sp.en_on = s.en_on;
+  if (s.en_on) sp.en_a = (R)s.theta[sp.off_en];
+  sp.nn_on = s.nn_on;
+  sp.pot_kind = s.pot_kind;
+  sp.half_omega2 = (R)(0.5 * s.omega * s.omega);
+  double vnn = 0.0;
+  for (int I = 0; I < s.n_nuc; ++I)
+    for (int K = I + 1; K < s.n_nuc; ++K) {
+      double d2 = 0.0;
+      for (int c = 0; c < 3; ++c) {
+        const double d = s.nuc_pos[3 * I + c] - s.nuc_pos[3 * K + c];
+        d2 += d * d;
+      }
+      vnn += (double)(s.nuc_z[I] * s.nuc_z[K]) / std::sqrt(d2);
+    }
+  sp.vnn = vnn;
+}
+
+void rebuild(mole_system& s) {
+  fill_params(s, s.sp64);
+  fill_params(s, s.sp32);
+}
+
+int grid_for(int W) { return (W + kBlock - 1) / kBlock; }
+
+int check_status(mole_ctx* ctx) {
+  int st = 0;
+  CUDA_TRY(cudaMemcpyAsync(&st, ctx->status.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  if (st & 2) return fail(MOLE_ERR_LINALG, "singular Slater matrix encountered");
+  if (st & 1) return fail(MOLE_ERR_FUNC, "non-finite local energy encountered");
+  return MOLE_OK;
+}
+
+struct Timer {
+  mole_ctx* ctx;
+  int kind;
+  Timer(mole_ctx* c, int k) : ctx(c), kind(k) {
+    if (ctx->timing) cudaEventRecord(ctx->ev0, ctx->stream);
+  }
+  void stop() {
+    if (!ctx->timing) return;
+    cudaEventRecord(ctx->ev1, ctx->stream);
+    cudaEventSynchronize(ctx->ev1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    ctx->kernel_ms[kind] += ms;
+    ctx->kernel_launches[kind] += 1;
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+int32_t mole_abi_version(void) { return MOLE_ABI_VERSION; }
+const char* mole_last_error_string(void) { return g_err.c_str(); }
+
+int mole_ctx_create(int32_t device, mole_ctx** out) {
+  if (!out) return fail(MOLE_ERR_INVALID_ARG, "out is NULL");
+  int n = 0;
+  CUDA_TRY(cudaGetDeviceCount(&n));
+  if (device < 0 || device >= n) return fail(MOLE_ERR_INVALID_ARG, "no such CUDA device");
+  CUDA_TRY(cudaSetDevice(device));
+  mole_ctx* c = new mole_ctx();
+  c->device = device;
+  cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, device);
+  cudaError_t e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+  if (e == cudaSuccess) e = c->status.reserve(1);
+  if (e != cudaSuccess) {
+    delete c;
+    return fail(MOLE_ERR_CUDA, std::string("context setup: ") + cudaGetErrorString(e));
+  }
+  c->stream = c->own;
+  *out = c;
+  return MOLE_OK;
+}
+
+int mole_ctx_destroy(mole_ctx* c) {
+  if (!c) return MOLE_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  c->partials.release();
+  c->tb_partials.release();
+  c->reduced.release();
+  c->scratch.release();
+  c->status.release();
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->own) cudaStreamDestroy(c->own);
+  delete c;
+  return MOLE_OK;
+}
+
+int mole_ctx_set_stream(mole_ctx* c, void* s) {
+  if (!c) return fail(MOLE_ERR_INVALID_ARG, "ctx is NULL");
+  c->stream = s ? (cudaStream_t)s : c->own;
+  return MOLE_OK;
+}
+
+int mole_sync(mole_ctx* c) {
+  if (!c) return fail(MOLE_ERR_INVALID_ARG, "ctx is NULL");
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return MOLE_OK;
+}
+
+int mole_ctx_enable_timing(mole_ctx* c, int32_t on) {
+  if (!c) return fail(MOLE_ERR_INVALID_ARG, "ctx is NULL");
+  c->timing = on != 0;
+  for (int k = 0; k < 3; ++k) {
+    c->kernel_ms[k] = 0;
+    c->kernel_launches[k] = 0;
+  }
+  return MOLE_OK;
+}
+
+int mole_ctx_kernel_time(mole_ctx* c, int32_t kernel, double* total_ms, int64_t* launches) {
+  if (!c || kernel < 0 || kernel > 2) return fail(MOLE_ERR_INVALID_ARG, "bad ctx or kernel id");
+  if (total_ms) *total_ms = c->kernel_ms[kernel];
+  if (launches) *launches = c->kernel_launches[kernel];
+  return MOLE_OK;
+}
+
+int mole_probe_peaks(mole_ctx* c, double* fp64, double* fp32) {
+  if (!c) return fail(MOLE_ERR_INVALID_ARG, "ctx is NULL");
+  CUDA_TRY(cudaSetDevice(c->device));
+  const int blocks = c->n_sm * 8, threads = 256;
+  CUDA_TRY(c->scratch.reserve((size_t)blocks * threads));
+  cudaEvent_t a, b;
+  CUDA_TRY(cudaEventCreate(&a));
+  CUDA_TRY(cudaEventCreate(&b));
+  double res[2] = {0, 0};
+  for (int k = 0; k < 2; ++k) {
+    const int iters = k == 0 ? 256 : 4096;
+    for (int rep = 0; rep < 3; ++rep) {
+      CUDA_TRY(cudaEventRecord(a, c->stream));
+      if (k == 0) CUDA_TRY(launch_fma_probe64(c->scratch.p, blocks, threads, iters, c->stream));
+      else CUDA_TRY(launch_fma_probe32((float*)c->scratch.p, blocks, threads, iters, c->stream));
+      CUDA_TRY(cudaEventRecord(b, c->stream));
+      CUDA_TRY(cudaEventSynchronize(b));
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, a, b);
+      const double flops = 2.0 * 64.0 * iters * (double)blocks * threads;
+      res[k] = std::max(res[k], flops / (ms * 1e-3) / 1e9);
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (fp64) *fp64 = res[0];
+  if (fp32) *fp32 = res[1];
+  return MOLE_OK;
+}
+
+int mole_system_create(mole_ctx* ctx, const mole_system_desc* d, const double* theta, int32_t n_theta,
+                       mole_system** out) {
+  if (!ctx || !d || !out) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
+  if (d->n_nuclei < 1 || d->n_nuclei > MOLE_MAX_NUCLEI) return fail(MOLE_ERR_SHAPE, "n_nuclei out of range");
+  if (d->n_up < 1 || d->n_up > MOLE_MAX_SPIN || d->n_dn < 0 || d->n_dn > d->n_up)
+    return fail(MOLE_ERR_SHAPE, "need 1 <= n_up <= 5 and 0 <= n_dn <= n_up");
+  if (d->n_basis < 1 || d->n_basis > MOLE_MAX_BASIS) return fail(MOLE_ERR_SHAPE, "n_basis out of range");
+  if (d->n_exp < 1 || d->n_exp > MOLE_MAX_BASIS) return fail(MOLE_ERR_SHAPE, "n_exp out of range");
+  if (d->ee_npoly < 0 || d->ee_npoly > MOLE_MAX_POLY) return fail(MOLE_ERR_SHAPE, "ee_npoly out of range");
+  if (!d->nuc_pos || !d->nuc_charge || !d->basis_center || !d->basis_kind || !d->basis_exp || !d->coef_up ||
+      (d->n_dn > 0 && !d->coef_dn) || (d->en_on && !d->en_coef))
+    return fail(MOLE_ERR_INVALID_ARG, "NULL descriptor array");
+  if (d->nn_on) return fail(MOLE_ERR_UNSUPPORTED, "neural Jastrow systems are created with mole_nn_system_create");
+  auto s = new mole_system();
+  s->ctx = ctx;
+  s->n_nuc = d->n_nuclei;
+  s->n_up = d->n_up;
+  s->n_dn = d->n_dn;
+  s->n_basis = d->n_basis;
+  s->n_exp = d->n_exp;
+  s->nuc_pos.assign(d->nuc_pos, d->nuc_pos + 3 * d->n_nuclei);
+  s->nuc_z.assign(d->nuc_charge, d->nuc_charge + d->n_nuclei);
+  s->b_center.assign(d->basis_center, d->basis_center + d->n_basis);
+  s->b_kind.assign(d->basis_kind, d->basis_kind + d->n_basis);
+  s->b_exp.assign(d->basis_exp, d->basis_exp + d->n_basis);
+  s->coef_up.assign(d->coef_up, d->coef_up + (size_t)d->n_up * d->n_basis);
+  if (d->n_dn > 0) s->coef_dn.assign(d->coef_dn, d->coef_dn + (size_t)d->n_dn * d->n_basis);
+  s->en_coef.assign(d->n_nuclei, 0.0);
+  if (d->en_on) s->en_coef.assign(d->en_coef, d->en_coef + d->n_nuclei);
+  for (int b = 0; b < d->n_basis; ++b) {
+    if (s->b_center[b] < 0 || s->b_center[b] >= d->n_nuclei || s->b_exp[b] < 0 || s->b_exp[b] >= d->n_exp ||
+        s->b_kind[b] < MOLE_STO_1S || s->b_kind[b] > MOLE_GTO_1S) {
+      delete s;
+      return fail(MOLE_ERR_SHAPE, "basis function index out of range");
+    }
+  }
+  s->ee_on = d->ee_on != 0;
+  s->ee_npoly = d->ee_on ? d->ee_npoly : 0;
+  s->ee_kappa = d->ee_kappa;
+  s->cusp_anti = d->cusp_anti;
+  s->cusp_para = d->cusp_para;
+  s->en_on = d->en_on != 0;
+  s->nn_on = 0;
+  s->pot_kind = d->pot_kind;
+  s->omega = d->omega;
+  s->P = s->n_exp + (s->ee_on ? 1 + s->ee_npoly : 0) + (s->en_on ? 1 : 0);
+  if (!theta || n_theta != s->P) {
+    const int P = s->P;
+    delete s;
+    return fail(MOLE_ERR_SHAPE, "theta must hold " + std::to_string(P) + " parameters");
+  }
+  s->theta.assign(theta, theta + n_theta);
+  s->k64 = kernel_set64(s->n_up, s->n_dn);
+  s->k32 = kernel_set32(s->n_up, s->n_dn);
+  if (!s->k64 || !s->k32) {
+    delete s;
+    return fail(MOLE_ERR_UNSUPPORTED, "no compiled kernels for this (n_up, n_dn); supported: n_dn = n_up or n_up - 1");
+  }
+  rebuild(*s);
+  *out = s;
+  return MOLE_OK;
+}
+
+int mole_system_destroy(mole_system* s) {
+  delete s;
+  return MOLE_OK;
+}
+
+int mole_num_params(const mole_system* s, int32_t* out) {
+  if (!s || !out) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
+  *out = s->P;
+  return MOLE_OK;
+}
+
+int mole_num_electrons(const mole_system* s, int32_t* out) {
+  if (!s || !out) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
+  *out = s->n_up + s->n_dn;
+  return MOLE_OK;
+}
+
+int mole_params_get(const mole_system* s, double* theta, int32_t n) {
+  if (!s || !theta) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
+  if (n != s->P) return fail(MOLE_ERR_SHAPE, "parameter count mismatch");
+  std::memcpy(theta, s->theta.data(), sizeof(double) * n);
+  return MOLE_OK;
+}
+
+int mole_params_set(mole_system* s, const double* theta, int32_t n) {
+  if (!s || !theta) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
+  if (n != s->P) return fail(MOLE_ERR_SHAPE, "parameter count mismatch");
+  s->theta.assign(theta, theta + n);
+  rebuild(*s);
+  return MOLE_OK;
+}
+
+int mole_walkers_create(mole_system* s, int32_t W, uint64_t seed, mole_walkers** out) {
+  if (!s || !out) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
+  if (W < 1) return fail(MOLE_ERR_SHAPE, "need at least one walker");
+  CUDA_TRY(cudaSetDevice(s->ctx->device));
+  auto w = new mole_walkers();
+  w->sys = s;
+  w->W = W;
+  w->seed = seed;
+  const size_t n = (size_t)W * 3 * (s->n_up + s->n_dn);
+  cudaError_t e = cudaMalloc(&w->pos, n * sizeof(double));
+  if (e != cudaSuccess) {
+    delete w;
+    return fail(MOLE_ERR_CUDA, std::string("walker positions: ") + cudaGetErrorString(e));
+  }
+  *out = w;
+  return mole_walkers_init(w, MOLE_INIT_NORMAL, 1.0);
+}
+
+static void free_dmc(mole_walkers* w) {
+  for (double** p : {&w->pos2, &w->eloc, &w->eloc2, &w->weight, &w->cum, &w->btot, &w->e_ref, &w->energies}) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+  }
+  if (w->dstep) cudaFree(w->dstep);
+  if (w->comb) cudaFree(w->comb);
+  w->dstep = nullptr;
+  w->comb = nullptr;
+  w->energies_n = 0;
+  w->eloc_valid = false;
+}
+
+int mole_walkers_destroy(mole_walkers* w) {
+  if (!w) return MOLE_OK;
+  cudaSetDevice(w->sys->ctx->device);
+  cudaStreamSynchronize(w->sys->ctx->stream);
+  if (w->pos) cudaFree(w->pos);
+  free_dmc(w);
+  delete w;
+  return MOLE_OK;
+}
+
+int mole_walkers_count(const mole_walkers* w, int32_t* out) {
+  if (!w || !out) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
+  *out = w->W;
+  return MOLE_OK;
+}
+
+int mole_walkers_init(mole_walkers* w, int32_t kind, double width) {
+  if (!w) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
+  if (kind != MOLE_INIT_NORMAL && kind != MOLE_INIT_UNIFORM) return fail(MOLE_ERR_INVALID_ARG, "bad init kind");
+  mole_ctx* c = w->sys->ctx;
+  CUDA_TRY(launch_init_positions(w->pos, w->W, w->sys->n_up + w->sys->n_dn, w->seed, kind, width, c->stream));
+  w->eloc_valid = false;
+  return MOLE_OK;
+}
+
+int mole_walkers_set_positions(mole_walkers* w, const double* pos, int64_t n) {
+  if (!w || !pos) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
+  const int NC = 3 * (w->sys->n_up + w->sys->n_dn);
+  if (n != (int64_t)w->W * NC) return fail(MOLE_ERR_SHAPE, "positions must hold W * N * 3 values");
+  mole_ctx* c = w->sys->ctx;
+  CUDA_TRY(c->scratch.reserve((size_t)n));
+  CUDA_TRY(cudaMemcpyAsync(c->scratch.p, pos, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(launch_aos_to_soa(c->scratch.p, w->pos, w->W, NC, c->stream));
+  w->eloc_valid = false;
+  return MOLE_OK;
+}
+
+int mole_walkers_get_positions(mole_walkers* w, double* pos, int64_t n) {
+  if (!w || !pos) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
+  const int NC = 3 * (w->sys->n_up + w->sys->n_dn);
+  if (n != (int64_t)w->W * NC) return fail(MOLE_ERR_SHAPE, "positions must hold W * N * 3 values");
+  mole_ctx* c = w->sys->ctx;
+  CUDA_TRY(c->scratch.reserve((size_t)n));
+  CUDA_TRY(launch_soa_to_aos(w->pos, c->scratch.p, w->W, NC, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(pos, c->scratch.p, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return MOLE_OK;
+}
+
+int mole_walkers_get_step(const mole_walkers* w, uint64_t* step) {
+  if (!w || !step) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
+  *step = w->step;
+  return MOLE_OK;
+}
+
+int mole_walkers_set_step(mole_walkers* w, uint64_t step) {
+  if (!w) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
+  w->step = step;
+  return MOLE_OK;
+}
+
+int mole_eval(mole_walkers* w, int32_t precision, double* lnpsi, double* sign, double* grad, double* lap,
+              double* eloc, double* O) {
+  if (!w) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
+  mole_system* s = w->sys;
+  mole_ctx* c = s->ctx;
+  const int W = w->W, N = s->n_up + s->n_dn, P = s->P;
+  if (P > 8 && O) return fail(MOLE_ERR_UNSUPPORTED, "O_k output supports at most 8 parameters here");
+  const size_t per = 5 + 3 * (size_t)N + P;
+  CUDA_TRY(c->reduced.reserve(per * W));
+  double* base = c->reduced.p;
+  EvalArgs a;
+  a.pos = w->pos;
+  a.W = W;
+  a.lnpsi = base;
+  a.sign = base + W;
+  a.lap = base + 2 * (size_t)W;
+  a.eloc = base + 3 * (size_t)W;
+  a.grad = base + 4 * (size_t)W;
+  a.O = a.grad + 3 * (size_t)N * W;
+  CUDA_TRY(cudaMemsetAsync(c->status.p, 0, sizeof(int), c->stream));
+  a.status = c->status.p;
+  Timer tm(c, 2);
+  if (precision == MOLE_PREC_MIXED) CUDA_TRY(s->k32->eval(s->sp32, a, grid_for(W), c->stream));
+  else CUDA_TRY(s->k64->eval(s->sp64, a, grid_for(W), c->stream));
+  tm.stop();
+  auto copy = [&](double* dst, const double* src, size_t n) -> int {
+    if (dst) CUDA_TRY(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    return MOLE_OK;
+  };
+  int rc;
+  if ((rc = copy(lnpsi, a.lnpsi, W)) || (rc = copy(sign, a.sign, W)) || (rc = copy(lap, a.lap, W)) ||
+      (rc = copy(eloc, a.eloc, W)) || (rc = copy(grad, a.grad, (size_t)3 * N * W)) ||
+      (rc = copy(O, a.O, (size_t)P * W)))
+    return rc;
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  const int st = check_status(c);
+  return st == MOLE_ERR_FUNC ? MOLE_OK : st;  // per-walker values are returned as computed
+}
+
+int mole_vmc_run(mole_walkers* w, const mole_vmc_opts* o, double* moments, double* time_blocks, double* sum_O,
+                 double* sum_EO, double* sum_OO) {
+  if (!w || !o || !moments) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
+  mole_system* s = w->sys;
+  mole_ctx* c = s->ctx;
+  if (o->block_size < 1 || o->n_steps < 0 || o->n_eq < 0 || o->n_steps % o->block_size != 0)
+    return fail(MOLE_ERR_SHAPE, "n_steps must be a non-negative multiple of block_size >= 1");
+  if (o->move < MOLE_MOVE_BOX || o->move > MOLE_MOVE_DIFFUSE || !(o->step > 0.0))
+    return fail(MOLE_ERR_INVALID_ARG, "bad move kind or step");
+  const int P = s->P;
+  int slot = 0;
+  if (o->sr) {
+    if (!sum_O || !sum_EO || !sum_OO) return fail(MOLE_ERR_DATA_ACCESS, "SR outputs are NULL");
+    const bool mixed = o->precision == MOLE_PREC_MIXED;
+    if (P <= 2 && (mixed ? s->k32->vmc[1][0] != nullptr : s->k64->vmc[1][0] != nullptr)) slot = 1;
+    else if (P <= 8) slot = 2;
+    else return fail(MOLE_ERR_UNSUPPORTED, "SR accumulation supports at most 8 parameters on this path");
+  }
+  const int PM = kPmWidth[slot];
+  const int drift = o->move == MOLE_MOVE_DIFFUSE ? 1 : 0;
+  const bool mixed = o->precision == MOLE_PREC_MIXED;
+  auto f64 = s->k64->vmc[slot][drift];
+  auto f32 = s->k32->vmc[slot][drift];
+  if (mixed ? !f32 : !f64) return fail(MOLE_ERR_UNSUPPORTED, "SR kernel not compiled for this family and precision");
+  const int W = w->W, grid = grid_for(W), NA = n_acc(PM);
+  const int n_tb = o->n_steps / o->block_size;
+  CUDA_TRY(c->partials.reserve((size_t)grid * NA));
+  CUDA_TRY(c->tb_partials.reserve((size_t)grid * std::max(n_tb, 1)));
+  CUDA_TRY(c->reduced.reserve((size_t)NA + std::max(n_tb, 1)));
+  CUDA_TRY(cudaMemsetAsync(c->status.p, 0, sizeof(int), c->stream));
+  VmcArgs a;
+  a.pos = w->pos;
+  a.W = W;
+  a.move = o->move;
+  a.step = o->step;
+  a.n_eq = o->n_eq;
+  a.n_steps = o->n_steps;
+  a.block_size = o->block_size;
+  a.refresh = o->refresh;
+  a.seed = w->seed;
+  a.step0 = (uint32_t)w->step;
+  a.partials = c->partials.p;
+  a.tb_partials = c->tb_partials.p;
+  a.status = c->status.p;
+  Timer tm(c, 0);
+  if (mixed) CUDA_TRY(f32(s->sp32, a, grid, c->stream));
+  else CUDA_TRY(f64(s->sp64, a, grid, c->stream));
+  tm.stop();
+  CUDA_TRY(launch_reduce_columns(c->partials.p, grid, NA, c->reduced.p, c->stream));
+  if (n_tb > 0) CUDA_TRY(launch_reduce_columns(c->tb_partials.p, grid, n_tb, c->reduced.p + NA, c->stream));
+  std::vector<double> h((size_t)NA + std::max(n_tb, 0));
+  CUDA_TRY(cudaMemcpyAsync(h.data(), c->reduced.p, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  w->step += (uint64_t)(o->n_eq + o->n_steps);
+  w->eloc_valid = false;
+  for (int k = 0; k < MOLE_NMOM; ++k) moments[k] = h[k];
+  if (time_blocks)
+    for (int k = 0; k < n_tb; ++k) time_blocks[k] = h[NA + k];
+  if (o->sr) {
+    for (int p = 0; p < P; ++p) {
+      sum_O[p] = h[kNMom + p];
+      sum_EO[p] = h[kNMom + PM + p];
+    }
+    int q = kNMom + 2 * PM;
+    for (int p = 0; p < PM; ++p)
+      for (int r = p; r < PM; ++r, ++q)
+        if (p < P && r < P) sum_OO[p * P + r] = sum_OO[r * P + p] = h[q];
+  }
+  return check_status(c);
+}
+
+int mole_sr_update(mole_ctx* ctx, int32_t P, double count, const double* sum_E, const double* sum_O,
+                   const double* sum_EO, const double* sum_OO, double eps, double step, double* delta,
+                   double* grad) {
+  if (!ctx || !sum_E || !sum_O || !sum_EO || !sum_OO || !delta) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
+  if (P < 1 || !(count > 0)) return fail(MOLE_ERR_SHAPE, "need P >= 1 and count > 0");
+  const double Eb = *sum_E / count;
+  std::vector<double> S((size_t)P * P), f(P), ob(P);
+  for (int k = 0; k < P; ++k) ob[k] = sum_O[k] / count;
+  for (int k = 0; k < P; ++k) {
+    const double g = 2.0 * (sum_EO[k] / count - Eb * ob[k]);
+    if (grad) grad[k] = g;
+    f[k] = -0.5 * g;
+    for (int l = 0; l < P; ++l) S[(size_t)k * P + l] = sum_OO[(size_t)k * P + l] / count - ob[k] * ob[l];
+    S[(size_t)k * P + k] += eps;
+  }
+  // Cholesky S = L L^T, then two triangular solves (FP64)
+  for (int j = 0; j < P; ++j) {
+    double d = S[(size_t)j * P + j];
+    for (int k = 0; k < j; ++k) d -= S[(size_t)j * P + k] * S[(size_t)j * P + k];
+    if (!(d > 0.0)) return fail(MOLE_ERR_LINALG, "SR matrix is not positive definite");
+    const double l = std::sqrt(d);
+    S[(size_t)j * P + j] = l;
+    for (int i = j + 1; i < P; ++i) {
+      double v = S[(size_t)i * P + j];
+      for (int k = 0; k < j; ++k) v -= S[(size_t)i * P + k] * S[(size_t)j * P + k];
+      S[(size_t)i * P + j] = v / l;
+    }
+  }
+  for (int i = 0; i < P; ++i) {
+    double v = f[i];
+    for (int k = 0; k < i; ++k) v -= S[(size_t)i * P + k] * f[k];
+    f[i] = v / S[(size_t)i * P + i];
+  }
+  for (int i = P - 1; i >= 0; --i) {
+    double v = f[i];
+    for (int k = i + 1; k < P; ++k) v -= S[(size_t)k * P + i] * f[k];
+    f[i] = v / S[(size_t)i * P + i];
+  }
+  for (int k = 0; k < P; ++k) delta[k] = step * f[k];
+  return MOLE_OK;
+}
+
+static int ensure_dmc(mole_walkers* w, int n_steps) {
+  mole_ctx* c = w->sys->ctx;
+  const int W = w->W, NC = 3 * (w->sys->n_up + w->sys->n_dn);
+  const int nb = (W + kScanBlock - 1) / kScanBlock;
+  if (!w->pos2) {
+    CUDA_TRY(cudaMalloc(&w->pos2, sizeof(double) * (size_t)W * NC));
+    CUDA_TRY(cudaMalloc(&w->eloc, sizeof(double) * W));
+    CUDA_TRY(cudaMalloc(&w->eloc2, sizeof(double) * W));
+    CUDA_TRY(cudaMalloc(&w->weight, sizeof(double) * W));
+    CUDA_TRY(cudaMalloc(&w->cum, sizeof(double) * W));
+    CUDA_TRY(cudaMalloc(&w->btot, sizeof(double) * nb));
+    CUDA_TRY(cudaMalloc(&w->e_ref, sizeof(double)));
+    CUDA_TRY(cudaMalloc(&w->dstep, sizeof(uint64_t)));
+    CUDA_TRY(cudaMalloc(&w->comb, sizeof(CombState)));
+  }
+  if (w->energies_n < (size_t)n_steps) {
+    if (w->energies) cudaFree(w->energies);
+    CUDA_TRY(cudaMalloc(&w->energies, sizeof(double) * n_steps));
+    w->energies_n = n_steps;
+  }
+  (void)c;
+  return MOLE_OK;
+}
+
+int mole_dmc_run(mole_walkers* w, const mole_dmc_opts* o, double* energies, double* accept) {
+  if (!w || !o) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
+  if (o->n_steps < 1 || !(o->tau > 0.0)) return fail(MOLE_ERR_SHAPE, "need n_steps >= 1 and tau > 0");
+  mole_system* s = w->sys;
+  mole_ctx* c = s->ctx;
+  const bool mixed = o->precision == MOLE_PREC_MIXED;
+  if (mixed ? !s->k32->dmc : !s->k64->dmc)
+    return fail(MOLE_ERR_UNSUPPORTED, "DMC kernels are compiled for up to four electrons");
+  const int W = w->W, NC = 3 * (s->n_up + s->n_dn), grid = grid_for(W);
+  const int nb = (W + kScanBlock - 1) / kScanBlock;
+  int rc = ensure_dmc(w, o->n_steps);
+  if (rc) return rc;
+  CUDA_TRY(c->partials.reserve((size_t)grid * 3));
+  CUDA_TRY(cudaMemsetAsync(c->status.p, 0, sizeof(int), c->stream));
+  if (!w->eloc_valid) {
+    // E_L at the current positions seeds E_L(old) of the first step
+    CUDA_TRY(c->reduced.reserve((size_t)(5 + NC) * W));
+    EvalArgs a;
+    a.pos = w->pos;
+    a.W = W;
+    a.lnpsi = c->reduced.p;
+    a.sign = a.lnpsi + W;
+    a.lap = a.sign + W;
+    a.eloc = w->eloc;
+    a.grad = a.lap + W;
+    a.O = nullptr;
+    a.status = c->status.p;
+    if (s->P > 0) {
+      CUDA_TRY(c->scratch.reserve((size_t)s->P * W));
+      a.O = c->scratch.p;
+    }
+    if (mixed) CUDA_TRY(s->k32->eval(s->sp32, a, grid, c->stream));
+    else CUDA_TRY(s->k64->eval(s->sp64, a, grid, c->stream));
+    w->eloc_valid = true;
+  }
+  const uint64_t step = w->step;
+  CombState cs0 = {0.0, 0.0, 0.0, 0.0};
+  CUDA_TRY(cudaMemcpyAsync(w->dstep, &step, sizeof(uint64_t), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(w->e_ref, &o->e_ref, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(w->comb, &cs0, sizeof(CombState), cudaMemcpyHostToDevice, c->stream));
+  DmcArgs a;
+  a.W = W;
+  a.tau = o->tau;
+  a.e_ref = w->e_ref;
+  a.seed = w->seed;
+  a.step = w->dstep;
+  a.partials = c->partials.p;
+  a.status = c->status.p;
+  a.weight = w->weight;
+  Timer tm(c, 1);
+  for (int t = 0; t < o->n_steps; ++t) {
+    a.pos = w->pos;
+    a.eloc = w->eloc;
+    if (mixed) CUDA_TRY(s->k32->dmc(s->sp32, a, grid, c->stream));
+    else CUDA_TRY(s->k64->dmc(s->sp64, a, grid, c->stream));
+    CUDA_TRY(launch_comb(w->weight, w->cum, w->btot, nb, c->partials.p, grid, w->comb, w->dstep, w->seed,
+                         w->energies, t, w->pos, w->eloc, w->pos2, w->eloc2, W, NC, c->stream));
+    std::swap(w->pos, w->pos2);
+    std::swap(w->eloc, w->eloc2);
+  }
+  tm.stop();
+  CombState cs;
+  if (energies)
+    CUDA_TRY(cudaMemcpyAsync(energies, w->energies, sizeof(double) * o->n_steps, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(&cs, w->comb, sizeof(CombState), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  w->step += (uint64_t)o->n_steps;
+  if (accept) {
+    accept[0] = cs.accepted;
+    accept[1] = cs.proposed;
+  }
+  return check_status(c);
+}
+
+// checkpoint: "MOLECKP1", W, N, P, seed, step, theta[P], positions [W][N][3]
+int mole_checkpoint_save(mole_walkers* w, const char* path) {
+  if (!w || !path) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
+  mole_system* s = w->sys;
+  const int N = s->n_up + s->n_dn;
+  std::vector<double> pos((size_t)w->W * N * 3);
+  int rc = mole_walkers_get_positions(w, pos.data(), (int64_t)pos.size());
+  if (rc) return rc;
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return fail(MOLE_ERR_IO, std::string("cannot open ") + path);
+  const char magic[8] = {'M', 'O', 'L', 'E', 'C', 'K', 'P', '1'};
+  const int64_t hdr[5] = {w->W, N, s->P, (int64_t)w->seed, (int64_t)w->step};
+  bool ok = std::fwrite(magic, 1, 8, f) == 8 && std::fwrite(hdr, sizeof(int64_t), 5, f) == 5 &&
+            std::fwrite(s->theta.data(), sizeof(double), s->P, f) == (size_t)s->P &&
+            std::fwrite(pos.data(), sizeof(double), pos.size(), f) == pos.size();
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? MOLE_OK : fail(MOLE_ERR_IO, "short write");
+}
+
+int mole_checkpoint_load(mole_walkers* w, const char* path) {
+  if (!w || !path) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
+  mole_system* s = w->sys;
+  const int N = s->n_up + s->n_dn;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(MOLE_ERR_IO, std::string("cannot open ") + path);
+  char magic[8];
+  int64_t hdr[5];
+  if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, "MOLECKP1", 8) != 0 ||
+      std::fread(hdr, sizeof(int64_t), 5, f) != 5) {
+    std::fclose(f);
+    return fail(MOLE_ERR_IO, "not a mole checkpoint");
+  }
+  if (hdr[0] != w->W || hdr[1] != N || hdr[2] != s->P) {
+    std::fclose(f);
+    return fail(MOLE_ERR_SHAPE, "checkpoint sizes do not match this walker set");
+  }
+  std::vector<double> theta(s->P), pos((size_t)w->W * N * 3);
+  const bool ok = std::fread(theta.data(), sizeof(double), s->P, f) == (size_t)s->P &&
+                  std::fread(pos.data(), sizeof(double), pos.size(), f) == pos.size();
+  std::fclose(f);
+  if (!ok) return fail(MOLE_ERR_IO, "truncated checkpoint");
+  int rc = mole_params_set(s, theta.data(), s->P);
+  if (rc) return rc;
+  w->seed = (uint64_t)hdr[3];
+  w->step = (uint64_t)hdr[4];
+  return mole_walkers_set_positions(w, pos.data(), (int64_t)pos.size());
+}
+
+}  // extern "C"

@@ -1,0 +1,6 @@
+// FP64 kernel instantiations for spin blocks of 1 up and 0 down electrons.
+#include "dispatch.cuh"
+
+namespace mole {
+MOLE_INSTANTIATE(1, 0, double, f64, true, true, true)
+}  // namespace mole

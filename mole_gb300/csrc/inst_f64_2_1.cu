@@ -1,0 +1,6 @@
+// FP64 kernel instantiations for spin blocks of 2 up and 1 down electrons.
+#include "dispatch.cuh"
+
+namespace mole {
+MOLE_INSTANTIATE(2, 1, double, f64, true, true, true)
+}  // namespace mole
