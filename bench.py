@@ -44,6 +44,7 @@ def parse():
     p.add_argument("--block", type=int, default=100)
     p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     p.add_argument("--no-extras", action="store_true", help="skip the e2e, mixed and CPU-baseline legs")
+    p.add_argument("--no-clocks", action="store_true", help="do not sample nvidia-smi during the timed region")
     return p.parse_args()
 
 
@@ -206,8 +207,11 @@ def main():
         sr_step(wf, sampler)
     ctx.enable_timing(True)
     clocks = ClockSampler(local)
-    clocks.start()
+    if not args.no_clocks:
+        clocks.start()
+    host_t0 = time.perf_counter()
     ms = timed(lambda: results.append(sr_step(wf, sampler)), args.steps)
+    host_s = time.perf_counter() - host_t0
     clk = clocks.stop()
     k_ms, k_n = ctx.kernel_time(0)
     ctx.enable_timing(False)
@@ -224,7 +228,8 @@ def main():
     roofline = {"bound": "fp64" if prec == api.PREC_FP64 else "fp32", "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
                 "kernel": "vmc_kernel<1,1,double,2,false>" if prec == api.PREC_FP64 else "vmc_kernel<1,1,float,2,false>",
-                "kernel_ms_per_launch": k_ms / k_n, "flops_per_walker_step": work.flops,
+                "kernel_ms_per_launch": k_ms / k_n, "kernel_share_of_step": k_ms / ms,
+                "host_wall_ms_per_step": 1e3 * host_s / args.steps, "flops_per_walker_step": work.flops,
                 "special_per_walker_step": work.special,
                 "peak_source": "measured live: FMA-chain probe (mole_probe_peaks)"}
 
@@ -276,9 +281,9 @@ def main():
             from oracle import oracle as O
 
             threads = O.hardware_threads()
-            rate, secs, _ = cpu_baseline_sample(threads, 256 * threads, 1000)
+            rate, secs, _ = cpu_baseline_sample(threads, 512 * threads, 2000)
             line["cpu_baseline"] = {"value": rate, "unit": "walker-steps/s", "cores": threads, "kind": "port",
-                                    "sample": f"{256 * threads} walkers x 1000 sweeps ({secs:.1f} s), reference call "
+                                    "sample": f"{512 * threads} walkers x 2000 sweeps ({secs:.1f} s), reference call "
                                               "pattern (oracle/faithful.cpp), std::thread over all host cores"}
     if rank == 0:
         print(json.dumps(line), flush=True)

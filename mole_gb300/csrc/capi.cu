@@ -80,6 +80,8 @@ struct mole_ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   DevBuf<double> partials, tb_partials, reduced, scratch;
   DevBuf<int> status;
+  int refs = 1;
+  bool closed = false;
 };
 
 struct mole_system {
@@ -95,6 +97,8 @@ struct mole_system {
   SysParams<float> sp32;
   const KernelSetT<double>* k64 = nullptr;
   const KernelSetT<float>* k32 = nullptr;
+  int refs = 1;
+  bool closed = false;
 };
 
 struct mole_walkers {
@@ -236,10 +240,13 @@ int mole_ctx_create(int32_t device, mole_ctx** out) {
   return MOLE_OK;
 }
 
-int mole_ctx_destroy(mole_ctx* c) {
-  if (!c) return MOLE_OK;
+// Handles are reference counted: a system keeps its context alive and a
+// walker set its system, so destroying them in any order is safe; the
+// memory goes when the last dependent handle is destroyed.
+static void release_ctx(mole_ctx* c) {
+  if (--c->refs > 0) return;
   cudaSetDevice(c->device);
-  cudaStreamSynchronize(c->stream);
+  cudaStreamSynchronize(c->own);
   c->partials.release();
   c->tb_partials.release();
   c->reduced.release();
@@ -248,7 +255,22 @@ int mole_ctx_destroy(mole_ctx* c) {
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->own) cudaStreamDestroy(c->own);
+  cudaGetLastError();  // teardown errors are not reported to later calls
   delete c;
+}
+
+static void release_sys(mole_system* s) {
+  if (--s->refs > 0) return;
+  mole_ctx* c = s->ctx;
+  delete s;
+  release_ctx(c);
+}
+
+int mole_ctx_destroy(mole_ctx* c) {
+  if (!c || c->closed) return MOLE_OK;
+  c->closed = true;
+  if (c->stream != c->own) c->stream = c->own;
+  release_ctx(c);
   return MOLE_OK;
 }
 
@@ -282,6 +304,7 @@ int mole_ctx_kernel_time(mole_ctx* c, int32_t kernel, double* total_ms, int64_t*
 }
 
 int mole_probe_peaks(mole_ctx* c, double* fp64, double* fp32) {
+  cudaGetLastError();  // report only errors raised by this call
   if (!c) return fail(MOLE_ERR_INVALID_ARG, "ctx is NULL");
   CUDA_TRY(cudaSetDevice(c->device));
   const int blocks = c->n_sm * 8, threads = 256;
@@ -370,12 +393,15 @@ int mole_system_create(mole_ctx* ctx, const mole_system_desc* d, const double* t
     return fail(MOLE_ERR_UNSUPPORTED, "no compiled kernels for this (n_up, n_dn); supported: n_dn = n_up or n_up - 1");
   }
   rebuild(*s);
+  ctx->refs += 1;
   *out = s;
   return MOLE_OK;
 }
 
 int mole_system_destroy(mole_system* s) {
-  delete s;
+  if (!s || s->closed) return MOLE_OK;
+  s->closed = true;
+  release_sys(s);
   return MOLE_OK;
 }
 
@@ -410,6 +436,7 @@ int mole_walkers_create(mole_system* s, int32_t W, uint64_t seed, mole_walkers**
   if (!s || !out) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
   if (W < 1) return fail(MOLE_ERR_SHAPE, "need at least one walker");
   CUDA_TRY(cudaSetDevice(s->ctx->device));
+  cudaGetLastError();  // a launch below reports its own error, not an earlier one
   auto w = new mole_walkers();
   w->sys = s;
   w->W = W;
@@ -420,8 +447,14 @@ int mole_walkers_create(mole_system* s, int32_t W, uint64_t seed, mole_walkers**
     delete w;
     return fail(MOLE_ERR_CUDA, std::string("walker positions: ") + cudaGetErrorString(e));
   }
+  s->refs += 1;
+  const int rc = mole_walkers_init(w, MOLE_INIT_NORMAL, 1.0);
+  if (rc != MOLE_OK) {
+    mole_walkers_destroy(w);
+    return rc;
+  }
   *out = w;
-  return mole_walkers_init(w, MOLE_INIT_NORMAL, 1.0);
+  return MOLE_OK;
 }
 
 static void free_dmc(mole_walkers* w) {
@@ -439,11 +472,14 @@ static void free_dmc(mole_walkers* w) {
 
 int mole_walkers_destroy(mole_walkers* w) {
   if (!w) return MOLE_OK;
-  cudaSetDevice(w->sys->ctx->device);
-  cudaStreamSynchronize(w->sys->ctx->stream);
+  mole_system* s = w->sys;
+  cudaSetDevice(s->ctx->device);
+  cudaStreamSynchronize(s->ctx->stream);
   if (w->pos) cudaFree(w->pos);
   free_dmc(w);
+  cudaGetLastError();  // teardown errors are not reported to later calls
   delete w;
+  release_sys(s);
   return MOLE_OK;
 }
 
@@ -454,6 +490,7 @@ int mole_walkers_count(const mole_walkers* w, int32_t* out) {
 }
 
 int mole_walkers_init(mole_walkers* w, int32_t kind, double width) {
+  cudaGetLastError();  // report only errors raised by this call
   if (!w) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
   if (kind != MOLE_INIT_NORMAL && kind != MOLE_INIT_UNIFORM) return fail(MOLE_ERR_INVALID_ARG, "bad init kind");
   mole_ctx* c = w->sys->ctx;
@@ -463,6 +500,7 @@ int mole_walkers_init(mole_walkers* w, int32_t kind, double width) {
 }
 
 int mole_walkers_set_positions(mole_walkers* w, const double* pos, int64_t n) {
+  cudaGetLastError();  // report only errors raised by this call
   if (!w || !pos) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
   const int NC = 3 * (w->sys->n_up + w->sys->n_dn);
   if (n != (int64_t)w->W * NC) return fail(MOLE_ERR_SHAPE, "positions must hold W * N * 3 values");
@@ -475,6 +513,7 @@ int mole_walkers_set_positions(mole_walkers* w, const double* pos, int64_t n) {
 }
 
 int mole_walkers_get_positions(mole_walkers* w, double* pos, int64_t n) {
+  cudaGetLastError();  // report only errors raised by this call
   if (!w || !pos) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
   const int NC = 3 * (w->sys->n_up + w->sys->n_dn);
   if (n != (int64_t)w->W * NC) return fail(MOLE_ERR_SHAPE, "positions must hold W * N * 3 values");
@@ -500,6 +539,7 @@ int mole_walkers_set_step(mole_walkers* w, uint64_t step) {
 
 int mole_eval(mole_walkers* w, int32_t precision, double* lnpsi, double* sign, double* grad, double* lap,
               double* eloc, double* O) {
+  cudaGetLastError();  // report only errors raised by this call
   if (!w) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
   mole_system* s = w->sys;
   mole_ctx* c = s->ctx;
@@ -539,6 +579,7 @@ int mole_eval(mole_walkers* w, int32_t precision, double* lnpsi, double* sign, d
 
 int mole_vmc_run(mole_walkers* w, const mole_vmc_opts* o, double* moments, double* time_blocks, double* sum_O,
                  double* sum_EO, double* sum_OO) {
+  cudaGetLastError();  // report only errors raised by this call
   if (!w || !o || !moments) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
   mole_system* s = w->sys;
   mole_ctx* c = s->ctx;
@@ -675,6 +716,7 @@ static int ensure_dmc(mole_walkers* w, int n_steps) {
 }
 
 int mole_dmc_run(mole_walkers* w, const mole_dmc_opts* o, double* energies, double* accept) {
+  cudaGetLastError();  // report only errors raised by this call
   if (!w || !o) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
   if (o->n_steps < 1 || !(o->tau > 0.0)) return fail(MOLE_ERR_SHAPE, "need n_steps >= 1 and tau > 0");
   mole_system* s = w->sys;
