@@ -560,8 +560,8 @@ int mole_eval(mole_walkers* w, int32_t precision, double* lnpsi, double* sign, d
   CUDA_TRY(cudaMemsetAsync(c->status.p, 0, sizeof(int), c->stream));
   a.status = c->status.p;
   Timer tm(c, 2);
-  if (precision == MOLE_PREC_MIXED) CUDA_TRY(s->k32->eval(s->sp32, a, grid_for(W), c->stream));
-  else CUDA_TRY(s->k64->eval(s->sp64, a, grid_for(W), c->stream));
+  if (precision == MOLE_PREC_MIXED) CUDA_TRY(s->k32->eval[s->en_on](s->sp32, a, grid_for(W), c->stream));
+  else CUDA_TRY(s->k64->eval[s->en_on](s->sp64, a, grid_for(W), c->stream));
   tm.stop();
   auto copy = [&](double* dst, const double* src, size_t n) -> int {
     if (dst) CUDA_TRY(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
@@ -592,15 +592,17 @@ int mole_vmc_run(mole_walkers* w, const mole_vmc_opts* o, double* moments, doubl
   if (o->sr) {
     if (!sum_O || !sum_EO || !sum_OO) return fail(MOLE_ERR_DATA_ACCESS, "SR outputs are NULL");
     const bool mixed = o->precision == MOLE_PREC_MIXED;
-    if (P <= 2 && (mixed ? s->k32->vmc[1][0] != nullptr : s->k64->vmc[1][0] != nullptr)) slot = 1;
+    // the two-parameter kernels cache one orbital-exponent derivative
+    if (P <= 2 && s->n_exp <= 1 && (mixed ? s->k32->vmc[1][0][0] != nullptr : s->k64->vmc[1][0][0] != nullptr))
+      slot = 1;
     else if (P <= 8) slot = 2;
     else return fail(MOLE_ERR_UNSUPPORTED, "SR accumulation supports at most 8 parameters on this path");
   }
   const int PM = kPmWidth[slot];
   const int drift = o->move == MOLE_MOVE_DIFFUSE ? 1 : 0;
   const bool mixed = o->precision == MOLE_PREC_MIXED;
-  auto f64 = s->k64->vmc[slot][drift];
-  auto f32 = s->k32->vmc[slot][drift];
+  auto f64 = s->k64->vmc[slot][drift][s->en_on];
+  auto f32 = s->k32->vmc[slot][drift][s->en_on];
   if (mixed ? !f32 : !f64) return fail(MOLE_ERR_UNSUPPORTED, "SR kernel not compiled for this family and precision");
   const int W = w->W, grid = grid_for(W), NA = n_acc(PM);
   const int n_tb = o->n_steps / o->block_size;
@@ -722,7 +724,7 @@ int mole_dmc_run(mole_walkers* w, const mole_dmc_opts* o, double* energies, doub
   mole_system* s = w->sys;
   mole_ctx* c = s->ctx;
   const bool mixed = o->precision == MOLE_PREC_MIXED;
-  if (mixed ? !s->k32->dmc : !s->k64->dmc)
+  if (mixed ? !s->k32->dmc[s->en_on] : !s->k64->dmc[s->en_on])
     return fail(MOLE_ERR_UNSUPPORTED, "DMC kernels are compiled for up to four electrons");
   const int W = w->W, NC = 3 * (s->n_up + s->n_dn), grid = grid_for(W);
   const int nb = (W + kScanBlock - 1) / kScanBlock;
@@ -747,8 +749,8 @@ int mole_dmc_run(mole_walkers* w, const mole_dmc_opts* o, double* energies, doub
       CUDA_TRY(c->scratch.reserve((size_t)s->P * W));
       a.O = c->scratch.p;
     }
-    if (mixed) CUDA_TRY(s->k32->eval(s->sp32, a, grid, c->stream));
-    else CUDA_TRY(s->k64->eval(s->sp64, a, grid, c->stream));
+    if (mixed) CUDA_TRY(s->k32->eval[s->en_on](s->sp32, a, grid, c->stream));
+    else CUDA_TRY(s->k64->eval[s->en_on](s->sp64, a, grid, c->stream));
     w->eloc_valid = true;
   }
   const uint64_t step = w->step;
@@ -769,8 +771,8 @@ int mole_dmc_run(mole_walkers* w, const mole_dmc_opts* o, double* energies, doub
   for (int t = 0; t < o->n_steps; ++t) {
     a.pos = w->pos;
     a.eloc = w->eloc;
-    if (mixed) CUDA_TRY(s->k32->dmc(s->sp32, a, grid, c->stream));
-    else CUDA_TRY(s->k64->dmc(s->sp64, a, grid, c->stream));
+    if (mixed) CUDA_TRY(s->k32->dmc[s->en_on](s->sp32, a, grid, c->stream));
+    else CUDA_TRY(s->k64->dmc[s->en_on](s->sp64, a, grid, c->stream));
     CUDA_TRY(launch_comb(w->weight, w->cum, w->btot, nb, c->partials.p, grid, w->comb, w->dstep, w->seed,
                          w->energies, t, w->pos, w->eloc, w->pos2, w->eloc2, W, NC, c->stream));
     std::swap(w->pos, w->pos2);

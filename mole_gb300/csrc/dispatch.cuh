@@ -14,49 +14,50 @@ struct KernelSetT {
   using Vmc = cudaError_t (*)(const SysParams<R>&, const VmcArgs&, int, cudaStream_t);
   using Eval = cudaError_t (*)(const SysParams<R>&, const EvalArgs&, int, cudaStream_t);
   using Dmc = cudaError_t (*)(const SysParams<R>&, const DmcArgs&, int, cudaStream_t);
-  Vmc vmc[kPmSlots][2];  // [PM slot][drift]; NULL where not compiled
-  Eval eval;
-  Dmc dmc;
+  Vmc vmc[kPmSlots][2][2];  // [PM slot][drift][e-n Jastrow]; NULL where not compiled
+  Eval eval[2];             // [e-n Jastrow]
+  Dmc dmc[2];               // [e-n Jastrow]; NULL where not compiled
 };
 
-template <int NU, int ND, class R, int PM, bool DRIFT>
+template <int NU, int ND, class R, int PM, bool DRIFT, bool EN>
 cudaError_t launch_vmc(const SysParams<R>& sp, const VmcArgs& a, int grid, cudaStream_t s) {
-  vmc_kernel<NU, ND, R, PM, DRIFT><<<grid, kBlock, 0, s>>>(sp, a);
+  vmc_kernel<NU, ND, R, PM, DRIFT, EN><<<grid, kBlock, 0, s>>>(sp, a);
   return cudaGetLastError();
 }
-template <int NU, int ND, class R>
+template <int NU, int ND, class R, bool EN>
 cudaError_t launch_eval(const SysParams<R>& sp, const EvalArgs& a, int grid, cudaStream_t s) {
-  eval_kernel<NU, ND, R, 8><<<grid, kBlock, 0, s>>>(sp, a);
+  eval_kernel<NU, ND, R, 8, EN><<<grid, kBlock, 0, s>>>(sp, a);
   return cudaGetLastError();
 }
-template <int NU, int ND, class R>
+template <int NU, int ND, class R, bool EN>
 cudaError_t launch_dmc(const SysParams<R>& sp, const DmcArgs& a, int grid, cudaStream_t s) {
-  dmc_step_kernel<NU, ND, R><<<grid, kBlock, 0, s>>>(sp, a);
+  dmc_step_kernel<NU, ND, R, EN><<<grid, kBlock, 0, s>>>(sp, a);
   return cudaGetLastError();
 }
 
-template <int NU, int ND, class R, int PM, bool DRIFT, bool ON>
+template <int NU, int ND, class R, int PM, bool DRIFT, bool EN, bool ON>
 typename KernelSetT<R>::Vmc maybe_vmc() {
-  if constexpr (ON) return launch_vmc<NU, ND, R, PM, DRIFT>;
+  if constexpr (ON) return launch_vmc<NU, ND, R, PM, DRIFT, EN>;
   else return nullptr;
 }
-template <int NU, int ND, class R, bool ON>
+template <int NU, int ND, class R, bool EN, bool ON>
 typename KernelSetT<R>::Dmc maybe_dmc() {
-  if constexpr (ON) return launch_dmc<NU, ND, R>;
+  if constexpr (ON) return launch_dmc<NU, ND, R, EN>;
   else return nullptr;
 }
 
 // SR2: compile the exact two-parameter SR kernels (the H2 optimisation);
-// SR8: the eight-wide SR kernels; DRIFT: drift-diffusion VMC and DMC
-// kernels (compiled for up to four electrons).
+// SR8: the eight-wide SR kernels; DRIFT: drift-diffusion VMC and DMC.
+#define MOLE_VMC_EN(NU, ND, R, PM, ON, DRIFT)                                                             \
+  {{maybe_vmc<NU, ND, R, PM, false, false, ON>(), maybe_vmc<NU, ND, R, PM, false, true, ON>()},          \
+   {maybe_vmc<NU, ND, R, PM, true, false, (ON && DRIFT)>(), maybe_vmc<NU, ND, R, PM, true, true, (ON && DRIFT)>()}}
 #define MOLE_INSTANTIATE(NU, ND, R, TAG, SR2, SR8, DRIFT)                                                 \
   const KernelSetT<R>* kernels_##TAG##_##NU##_##ND() {                                                   \
     static const KernelSetT<R> ks = {                                                                    \
-        {{maybe_vmc<NU, ND, R, 0, false, true>(), maybe_vmc<NU, ND, R, 0, true, DRIFT>()},               \
-         {maybe_vmc<NU, ND, R, 2, false, SR2>(), maybe_vmc<NU, ND, R, 2, true, (SR2 && DRIFT)>()},        \
-         {maybe_vmc<NU, ND, R, 8, false, SR8>(), maybe_vmc<NU, ND, R, 8, true, (SR8 && DRIFT)>()}},       \
-        launch_eval<NU, ND, R>,                                                                          \
-        maybe_dmc<NU, ND, R, DRIFT>()};                                                                  \
+        {MOLE_VMC_EN(NU, ND, R, 0, true, DRIFT), MOLE_VMC_EN(NU, ND, R, 2, SR2, DRIFT),                   \
+         MOLE_VMC_EN(NU, ND, R, 8, SR8, DRIFT)},                                                         \
+        {launch_eval<NU, ND, R, false>, launch_eval<NU, ND, R, true>},                                   \
+        {maybe_dmc<NU, ND, R, false, DRIFT>(), maybe_dmc<NU, ND, R, true, DRIFT>()}};                    \
     return &ks;                                                                                          \
   }
 

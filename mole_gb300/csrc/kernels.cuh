@@ -5,6 +5,15 @@
 
 namespace mole {
 
+// Threads per CTA for every walker kernel, and the resident CTAs per SM the
+// register budget is tuned for: seven 64-walker CTAs per SM hold 65,536
+// walkers in one balanced wave on 152 SMs.
+constexpr int kBlock = 64;
+template <int NU, int ND>
+constexpr int min_blocks() {
+  return (NU + ND) <= 2 ? 7 : ((NU + ND) <= 4 ? 4 : 2);
+}
+
 // Accumulators per walker: moments first, then SR sums.
 constexpr int kNMom = 7;  // count, sumE, sumE2, sumBlock2, nBlocks, accept, proposed
 __host__ __device__ constexpr int n_acc(int PM) { return kNMom + (PM > 0 ? 2 * PM + PM * (PM + 1) / 2 : 0); }
@@ -22,97 +31,94 @@ struct VmcArgs {
   int* status;          // bit 0: non-finite E_L; bit 1: singular determinant
 };
 
-template <int NU, int ND, class R, int PM, int MOVE>
-__device__ __forceinline__ void vmc_body(const SysParams<R>& sp, const VmcArgs& a, double* red) {
-  using Wk = Walker<NU, ND, R>;
+// The energy sums live in registers; the SR sums, touched once per sweep,
+// live in per-thread shared-memory slots srs[k * blockDim.x + tid] to keep
+// the walker caches in registers.
+template <int NU, int ND, class R, int PM, bool EN, int MOVE>
+__device__ __forceinline__ void vmc_body(const SysParams<R>& sp, const VmcArgs& a, double* red, double* srs) {
+  using Wk = Walker<NU, ND, R, PM, EN>;
   constexpr int NA = n_acc(PM);
+  constexpr int NSR = NA - kNMom;
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  const int tid = threadIdx.x;
   const bool active = w < a.W;
   Wk wk;
   if (active) wk.load(a.pos, a.W, w);
   else
 #pragma unroll
     for (int e = 0; e < Wk::N; ++e) wk.x[e][0] = wk.x[e][1] = wk.x[e][2] = 1.0 + e;
-  bool ok = wk.template refresh<MOVE == kMoveDiffuse>(sp, nullptr, nullptr);
-  double acc[NA];
+  bool ok = wk.refresh(sp, nullptr, nullptr);
+  double sE = 0.0, sE2 = 0.0, sB2 = 0.0, bsum = 0.0;
+  int naccept = 0;
 #pragma unroll
-  for (int k = 0; k < NA; ++k) acc[k] = 0.0;
-  double bsum = 0.0;
+  for (int k = 0; k < NSR; ++k) srs[k * kBlock + tid] = 0.0;
   const int total = a.n_eq + a.n_steps;
   const int refresh = a.refresh > 0 ? a.refresh : 100;
   const R step = (R)a.step;
   for (int it = 0; it < total; ++it) {
     const uint32_t t = a.step0 + (uint32_t)it;
-    acc[5] += (double)wk.template sweep<MOVE>(sp, step, a.seed, (uint32_t)w, t);
-    if ((it + 1) % refresh == 0) ok = wk.template refresh<MOVE == kMoveDiffuse>(sp, nullptr, nullptr) && ok;
+    naccept += wk.template sweep<MOVE>(sp, step, a.seed, (uint32_t)w, t);
+    if ((it + 1) % refresh == 0) ok = wk.refresh(sp, nullptr, nullptr) && ok;
     if (it < a.n_eq) continue;
     double O[PM > 0 ? PM : 1];
-    const double E = wk.template local_energy<PM>(sp, O, nullptr, nullptr);
+    const double E = wk.local_energy(sp, O, nullptr, nullptr);
     const int k = it - a.n_eq;
-    acc[0] += 1.0;
-    acc[1] += E;
-    acc[2] += E * E;
+    sE += E;
+    sE2 += E * E;
     bsum += E;
     if constexpr (PM > 0) {
 #pragma unroll
       for (int p = 0; p < PM; ++p) {
-        acc[kNMom + p] += O[p];
-        acc[kNMom + PM + p] += E * O[p];
+        srs[p * kBlock + tid] += O[p];
+        srs[(PM + p) * kBlock + tid] += E * O[p];
       }
-      int q = kNMom + 2 * PM;
+      int q = 2 * PM;
 #pragma unroll
       for (int p = 0; p < PM; ++p)
 #pragma unroll
-        for (int r = p; r < PM; ++r) acc[q++] += O[p] * O[r];
+        for (int r = p; r < PM; ++r, ++q) srs[q * kBlock + tid] += O[p] * O[r];
     }
     if ((k + 1) % a.block_size == 0) {
       const double m = bsum / a.block_size;
-      acc[3] += m * m;
-      acc[4] += 1.0;
+      sB2 += m * m;
       double v[1] = {active ? bsum : 0.0};
       block_sum<1>(v, red);
       if (threadIdx.x == 0) a.tb_partials[(size_t)blockIdx.x * (a.n_steps / a.block_size) + k / a.block_size] = v[0];
       bsum = 0.0;
     }
   }
-  acc[6] = (double)total * Wk::N;
+  double acc[kNMom] = {(double)a.n_steps, sE, sE2, sB2, (double)(a.n_steps / a.block_size), (double)naccept,
+                       (double)total * Wk::N};
   if (active) {
     wk.store(a.pos, a.W, w);
     if (!ok) atomicOr(a.status, 2);
-    if (!(acc[1] == acc[1]) || !(acc[2] < 1e300)) atomicOr(a.status, 1);
+    if (!(sE == sE) || !(sE2 < 1e300)) atomicOr(a.status, 1);
   } else {
 #pragma unroll
-    for (int k = 0; k < NA; ++k) acc[k] = 0.0;
+    for (int k = 0; k < kNMom; ++k) acc[k] = 0.0;
   }
   // deterministic CTA reduction, then one partial row per CTA
 #pragma unroll
   for (int k = 0; k < NA; ++k) {
-    double v[1] = {acc[k]};
+    double v[1] = {k < kNMom ? acc[k] : (active ? srs[(k - kNMom) * kBlock + tid] : 0.0)};
     block_sum<1>(v, red);
     if (threadIdx.x == 0) a.partials[(size_t)blockIdx.x * NA + k] = v[0];
   }
 }
 
-// Threads per CTA for every walker kernel, and the resident CTAs per SM the
-// register budget is tuned for: seven 64-walker CTAs per SM hold 65,536
-// walkers in one balanced wave on 152 SMs.
-constexpr int kBlock = 64;
-template <int NU, int ND>
-constexpr int min_blocks() {
-  return (NU + ND) <= 2 ? 7 : ((NU + ND) <= 4 ? 4 : 2);
-}
 
 // DRIFT selects the drift-diffusion kernel; otherwise box and Gaussian moves
 // share one kernel (uniform branch on a.move).
-template <int NU, int ND, class R, int PM, bool DRIFT>
+template <int NU, int ND, class R, int PM, bool DRIFT, bool EN>
 __global__ void __launch_bounds__(kBlock, (min_blocks<NU, ND>())) vmc_kernel(const __grid_constant__ SysParams<R> sp,
                                                                             const VmcArgs a) {
   __shared__ double red[kBlock / 32];
+  __shared__ double srs[(n_acc(PM) - kNMom > 0 ? n_acc(PM) - kNMom : 1) * kBlock];
   if constexpr (DRIFT) {
-    vmc_body<NU, ND, R, PM, kMoveDiffuse>(sp, a, red);
+    vmc_body<NU, ND, R, PM, EN, kMoveDiffuse>(sp, a, red, srs);
   } else {
-    if (a.move == kMoveBox) vmc_body<NU, ND, R, PM, kMoveBox>(sp, a, red);
-    else vmc_body<NU, ND, R, PM, kMoveGauss>(sp, a, red);
+    if (a.move == kMoveBox) vmc_body<NU, ND, R, PM, EN, kMoveBox>(sp, a, red, srs);
+    else vmc_body<NU, ND, R, PM, EN, kMoveGauss>(sp, a, red, srs);
   }
 }
 
@@ -128,19 +134,19 @@ struct EvalArgs {
   int* status;
 };
 
-template <int NU, int ND, class R, int PM>
+template <int NU, int ND, class R, int PM, bool EN>
 __global__ void __launch_bounds__(kBlock) eval_kernel(const __grid_constant__ SysParams<R> sp, const EvalArgs a) {
-  using Wk = Walker<NU, ND, R>;
+  using Wk = Walker<NU, ND, R, PM, EN>;
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
   if (w >= a.W) return;
   Wk wk;
   wk.load(a.pos, a.W, w);
   double ln, sg;
-  const bool ok = wk.template refresh<false>(sp, &ln, &sg);
+  const bool ok = wk.refresh(sp, &ln, &sg);
   double O[PM > 0 ? PM : 1];
   double g[Wk::N * 3];
   double lap;
-  const double E = wk.template local_energy<PM>(sp, O, g, &lap);
+  const double E = wk.local_energy(sp, O, g, &lap);
   if (!ok) atomicOr(a.status, 2);
   if (!(E == E)) atomicOr(a.status, 1);
   a.lnpsi[w] = ln;
@@ -166,9 +172,9 @@ struct DmcArgs {
   int* status;
 };
 
-template <int NU, int ND, class R>
+template <int NU, int ND, class R, bool EN>
 __global__ void __launch_bounds__(kBlock, (min_blocks<NU, ND>())) dmc_step_kernel(const __grid_constant__ SysParams<R> sp, const DmcArgs a) {
-  using Wk = Walker<NU, ND, R>;
+  using Wk = Walker<NU, ND, R, 0, EN>;
   __shared__ double red[3 * kBlock / 32];
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = w < a.W;
@@ -177,11 +183,11 @@ __global__ void __launch_bounds__(kBlock, (min_blocks<NU, ND>())) dmc_step_kerne
   if (active) {
     Wk wk;
     wk.load(a.pos, a.W, w);
-    bool ok = wk.template refresh<true>(sp, nullptr, nullptr);
+    bool ok = wk.refresh(sp, nullptr, nullptr);
     const double e_old = a.eloc[w];
     const int nacc = wk.template sweep<kMoveDiffuse>(sp, (R)a.tau, a.seed, (uint32_t)w, t);
     double O[1];
-    const double e_new = wk.template local_energy<0>(sp, O, nullptr, nullptr);
+    const double e_new = wk.local_energy(sp, O, nullptr, nullptr);
     wk.store(a.pos, a.W, w);
     a.eloc[w] = e_new;
     a.weight[w] = exp(-a.tau * (0.5 * (e_old + e_new) - *a.e_ref));

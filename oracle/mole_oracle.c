@@ -61,6 +61,74 @@ static void box_muller(uint32_t a, uint32_t b, double* z0, double* z1) {
   *z1 = r * sin(t);
 }
 
+/* Single-precision Box-Muller whose every operation is an IEEE-rounded add,
+ * mul, fma, div or sqrt, in a fixed order (this file is compiled with
+ * -ffp-contract=off): ln u from u = m 2^e, m in [sqrt(1/2), sqrt(2)),
+ * ln m = 2 atanh(s), s = (m-1)/(m+1), series through s^9; sin/cos of an angle
+ * in one quadrant from their Taylor series through x^11 / x^12. The GPU path
+ * draws its proposal normals the same way, so both produce the same bits. */
+static float f32_log01(float u) {
+  uint32_t bits;
+  memcpy(&bits, &u, 4);
+  int e = (int)((bits >> 23) & 0xffu) - 127;
+  uint32_t mb = (bits & 0x7fffffu) | 0x3f800000u;
+  float m;
+  memcpy(&m, &mb, 4);
+  if (m > 1.41421356f) {
+    m = m * 0.5f;
+    e += 1;
+  }
+  const float s = (m - 1.0f) / (m + 1.0f);
+  const float s2 = s * s;
+  float p = fmaf(s2, 0.111111112f, 0.142857149f);
+  p = fmaf(p, s2, 0.2f);
+  p = fmaf(p, s2, 0.333333343f);
+  p = fmaf(p, s2, 1.0f);
+  const float t = s * p;
+  return fmaf((float)e, 0.693147182f, t + t);
+}
+
+static void f32_sincos_q(float x, float* s, float* c) {
+  const float x2 = x * x;
+  float ps = fmaf(x2, -2.50521084e-8f, 2.75573192e-6f);
+  ps = fmaf(ps, x2, -1.98412698e-4f);
+  ps = fmaf(ps, x2, 8.33333333e-3f);
+  ps = fmaf(ps, x2, -1.66666667e-1f);
+  ps = fmaf(ps, x2, 1.0f);
+  *s = x * ps;
+  float pc = fmaf(x2, 2.08767570e-9f, -2.75573192e-7f);
+  pc = fmaf(pc, x2, 2.48015873e-5f);
+  pc = fmaf(pc, x2, -1.38888889e-3f);
+  pc = fmaf(pc, x2, 4.16666667e-2f);
+  pc = fmaf(pc, x2, -0.5f);
+  *c = fmaf(pc, x2, 1.0f);
+}
+
+static void f32_box_muller(uint32_t a, uint32_t b, float* z0, float* z1) {
+  const float u = ((float)(a >> 8) + 0.5f) * 5.96046448e-8f;
+  const float r = sqrtf(-2.0f * f32_log01(u));
+  const float f = ((float)((b >> 6) & 0xffffffu) + 0.5f) * 5.96046448e-8f;
+  const float x = f * 1.57079637f;
+  float s, c;
+  f32_sincos_q(x, &s, &c);
+  const uint32_t q = b >> 30;
+  float cs = c, sn = s;
+  if (q == 1u) {
+    cs = -s;
+    sn = c;
+  } else if (q == 2u) {
+    cs = -c;
+    sn = -s;
+  } else if (q == 3u) {
+    cs = s;
+    sn = -c;
+  }
+  *z0 = r * cs;
+  *z1 = r * sn;
+}
+
+void orc_normal_pair(uint32_t a, uint32_t b, float* z) { f32_box_muller(a, b, &z[0], &z[1]); }
+
 void orc_init_positions(int W, int N, uint64_t seed, int kind, double width, double* pos) {
   for (int w = 0; w < W; ++w)
     for (int e = 0; e < N; ++e) {
@@ -572,16 +640,16 @@ static int move_electron(const orc_system* s, const double* th, int N, double* p
     for (int k = 0; k < 3; ++k) dx[k] = step * (u01(ua[k]) - 0.5);
     uacc = u01(ua[3]);
   } else {
-    double z[4];
-    box_muller(ua[0], ua[1], &z[0], &z[1]);
-    box_muller(ua[2], ua[3], &z[2], &z[3]);
+    float z[4];
+    f32_box_muller(ua[0], ua[1], &z[0], &z[1]);
+    f32_box_muller(ua[2], ua[3], &z[2], &z[3]);
     draw4(seed, walker, t, (uint32_t)(2 * e + 1), TAG_MOVE, ub);
     uacc = u01(ub[0]);
     if (move == ORC_MOVE_GAUSS) {
-      for (int k = 0; k < 3; ++k) dx[k] = step * z[k];
+      for (int k = 0; k < 3; ++k) dx[k] = step * (double)z[k];
     } else {
       double sq = sqrt(step);
-      for (int k = 0; k < 3; ++k) dx[k] = step * cur->grad[3 * e + k] + sq * z[k];
+      for (int k = 0; k < 3; ++k) dx[k] = step * cur->grad[3 * e + k] + sq * (double)z[k];
     }
   }
   for (int k = 0; k < 3; ++k) prop[3 * e + k] += dx[k];

@@ -75,6 +75,8 @@ typedef struct {
 } orc_eval_out;
 
 int orc_num_params(const orc_system* s);
+/* The proposal normals: two N(0,1) floats from 2 x 32 random bits. */
+void orc_normal_pair(uint32_t a, uint32_t b, float* z);
 void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 
 /* lnpsi, sign, grad ln psi, lap psi/psi, E_L and O_k = d ln psi / d theta_k

@@ -26,6 +26,28 @@ def test_philox_known_answers():
         0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]
 
 
+def test_proposal_normals_are_gaussian():
+    import ctypes as C
+
+    L = O.lib()
+    L.orc_normal_pair.argtypes = [C.c_uint32, C.c_uint32, C.POINTER(C.c_float)]
+    rng = np.random.default_rng(1)
+    a = rng.integers(0, 2 ** 32, size=40000, dtype=np.uint64)
+    b = rng.integers(0, 2 ** 32, size=40000, dtype=np.uint64)
+    z = np.zeros(2, dtype=np.float32)
+    out = np.zeros((a.size, 2))
+    for i in range(a.size):
+        L.orc_normal_pair(int(a[i]), int(b[i]), z.ctypes.data_as(C.POINTER(C.c_float)))
+        out[i] = z
+    u = ((a >> 8).astype(np.float64) + 0.5) * 2.0 ** -24
+    th = ((b >> 30).astype(np.float64) + (((b >> 6) & 0xFFFFFF).astype(np.float64) + 0.5) * 2.0 ** -24) * np.pi / 2
+    r = np.sqrt(-2.0 * np.log(u))
+    exact = np.stack([r * np.cos(th), r * np.sin(th)], axis=1)
+    assert np.max(np.abs(out - exact)) < 2e-5
+    x = out.reshape(-1)
+    assert abs(x.mean()) < 0.02 and abs(x.var() - 1.0) < 0.02 and abs((x ** 4).mean() - 3.0) < 0.1
+
+
 def test_sho_zero_variance():
     s = S.sho_gaussian(np.sqrt(2.0), 1.0)
     pos = np.random.default_rng(3).normal(size=(200, 1, 3)) * 1.5
