@@ -200,6 +200,29 @@ int mole_eval(mole_walkers* w, int32_t precision, double* lnpsi, double* sign, d
 int mole_vmc_run(mole_walkers* w, const mole_vmc_opts* opts, double* moments, double* time_blocks,
                  double* sum_O, double* sum_EO, double* sum_OO);
 
+/* Allocation-free variant of mole_vmc_run (no counterpart in the reference).
+ * For callers that cannot allocate device memory while they run: a host
+ * framework that owns all device memory through its own pool, or code that
+ * must not take cudaMalloc's implicit device synchronisation inside a timed or
+ * latency-critical loop. The caller passes every input and output as device
+ * memory: d_pos the positions as SoA float64 [3N][W] (updated in place),
+ * d_moments[MOLE_NMOM], d_time_blocks[n_steps / block_size] (may be NULL when
+ * n_steps is 0), d_sr = [sum_O (P), sum_EO (P), sum_OO (P x P)] when opts->sr
+ * (else may be NULL); seed and step0 select the random streams (the same
+ * streams mole_vmc_run uses for a walker set with that seed and step counter;
+ * the caller advances step0 by n_eq + n_steps itself). The library's only
+ * working memory is one fixed 2 MiB device array that every GPU loading the
+ * library holds until the process exits; the call is rejected with
+ * MOLE_ERR_SHAPE when ceil(W / 64) x (accumulators + time blocks) does not
+ * fit it. The first call on a device looks up that array's device address,
+ * so make it before any stream capture. Every call shares the array: calls
+ * that overlap on the GPU (other streams, other threads) race. The call
+ * synchronises `stream` (a cudaStream_t, NULL for the default stream) before
+ * returning. */
+int mole_vmc_run_noalloc(const mole_system* sys, double* d_pos, int32_t n_walkers, uint64_t seed, uint64_t step0,
+                         const mole_vmc_opts* opts, double* d_moments, double* d_time_blocks, double* d_sr,
+                         void* stream);
+
 /* StochasticReconfiguration::compute_parameter_update (src/optimize/src/optimizers.rs:236-252)
  * from the reduced sums of mole_vmc_run: S_kl = <O_k O_l> - <O_k><O_l>,
  * g_k = 2 (<E O_k> - <E><O_k>), S_kk += eps, delta = step * S^-1 (-g/2), FP64

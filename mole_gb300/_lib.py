@@ -85,6 +85,8 @@ SIGNATURES = {
     "mole_walkers_set_step": (C.c_int, [_P, C.c_uint64]),
     "mole_eval": (C.c_int, [_P, C.c_int32, _D, _D, _D, _D, _D, _D]),
     "mole_vmc_run": (C.c_int, [_P, C.POINTER(VmcOpts), _D, _D, _D, _D, _D]),
+    "mole_vmc_run_noalloc": (C.c_int, [_P, C.c_void_p, C.c_int32, C.c_uint64, C.c_uint64, C.POINTER(VmcOpts),
+                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mole_sr_update": (C.c_int, [_P, C.c_int32, C.c_double, _D, _D, _D, _D, C.c_double, C.c_double, _D, _D]),
     "mole_dmc_run": (C.c_int, [_P, C.POINTER(DmcOpts), _D, _D]),
     "mole_checkpoint_save": (C.c_int, [_P, C.c_char_p]),

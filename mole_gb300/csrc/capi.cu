@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -649,6 +650,108 @@ int mole_vmc_run(mole_walkers* w, const mole_vmc_opts* o, double* moments, doubl
         if (p < P && r < P) sum_OO[p * P + r] = sum_OO[r * P + p] = h[q];
   }
   return check_status(c);
+}
+
+}  // extern "C"
+
+// ------------------------------------------------- allocation-free VMC sweep
+//
+// Scratch of mole_vmc_run_noalloc: the per-CTA partial sums, the per-CTA
+// time-block sums, the reduced sums and the status word. It is a fixed
+// 2 MiB array that every GPU loading this library holds until the process
+// exits. In host code g_noalloc_scratch is only a stand-in for the symbol; the
+// device address comes from cudaGetSymbolAddress, once per device.
+static constexpr size_t kNoAllocScratchDoubles = (size_t)1 << 18;  // 2 MiB
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
+
+namespace {
+std::mutex g_noalloc_mu;
+double* g_noalloc_addr[256] = {nullptr};
+
+// Device address of the scratch array on `device` (which must be current).
+cudaError_t noalloc_scratch(int device, double** out) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (device < 0 || device >= 256) return cudaErrorInvalidDevice;
+  if (!g_noalloc_addr[device]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_noalloc_addr[device] = (double*)p;
+  }
+  *out = g_noalloc_addr[device];
+  return cudaSuccess;
+}
+}  // namespace
+
+extern "C" {
+
+int mole_vmc_run_noalloc(const mole_system* s, double* d_pos, int32_t W, uint64_t seed, uint64_t step0,
+                         const mole_vmc_opts* o, double* d_moments, double* d_time_blocks, double* d_sr,
+                         void* stream) {
+  if (!s || !d_pos || !o || !d_moments) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
+  if (W < 1) return fail(MOLE_ERR_SHAPE, "need at least one walker");
+  if (o->block_size < 1 || o->n_steps < 0 || o->n_eq < 0 || o->n_steps % o->block_size != 0)
+    return fail(MOLE_ERR_SHAPE, "n_steps must be a non-negative multiple of block_size >= 1");
+  if (o->move < MOLE_MOVE_BOX || o->move > MOLE_MOVE_DIFFUSE || !(o->step > 0.0))
+    return fail(MOLE_ERR_INVALID_ARG, "bad move kind or step");
+  const bool mixed = o->precision == MOLE_PREC_MIXED;
+  const int P = s->P;
+  int slot = 0;
+  if (o->sr) {
+    if (!d_sr) return fail(MOLE_ERR_DATA_ACCESS, "SR output is NULL");
+    if (P <= 2 && s->n_exp <= 1 && (mixed ? s->k32->vmc[1][0][0] != nullptr : s->k64->vmc[1][0][0] != nullptr))
+      slot = 1;
+    else if (P <= 8) slot = 2;
+    else return fail(MOLE_ERR_UNSUPPORTED, "SR accumulation supports at most 8 parameters on this path");
+  }
+  const int PM = kPmWidth[slot];
+  const int drift = o->move == MOLE_MOVE_DIFFUSE ? 1 : 0;
+  auto f64 = s->k64->vmc[slot][drift][s->en_on];
+  auto f32 = s->k32->vmc[slot][drift][s->en_on];
+  if (mixed ? !f32 : !f64) return fail(MOLE_ERR_UNSUPPORTED, "kernel not compiled for this family and precision");
+  const int grid = grid_for(W), NA = n_acc(PM), n_tb = o->n_steps / o->block_size;
+  // scratch layout: partials [grid][NA] | time-block partials [grid][n_tb] | reduced [NA] | status
+  const size_t need = (size_t)grid * NA + (size_t)grid * n_tb + NA + 1;
+  if (need > kNoAllocScratchDoubles)
+    return fail(MOLE_ERR_SHAPE, "walkers x (accumulators + time blocks) needs " + std::to_string(need * 8) +
+                                    " bytes of scratch; the allocation-free entry point has " +
+                                    std::to_string(kNoAllocScratchDoubles * 8));
+  if (n_tb > 0 && !d_time_blocks) return fail(MOLE_ERR_DATA_ACCESS, "time_blocks output is NULL");
+  CUDA_TRY(cudaSetDevice(s->ctx->device));
+  cudaGetLastError();  // report only errors raised by this call
+  double* scratch = nullptr;
+  CUDA_TRY(noalloc_scratch(s->ctx->device, &scratch));
+  cudaStream_t st = (cudaStream_t)stream;
+  double* partials = scratch;
+  double* tb_partials = partials + (size_t)grid * NA;
+  double* reduced = tb_partials + (size_t)grid * n_tb;
+  int* status = (int*)(reduced + NA);
+  CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), st));
+  VmcArgs a;
+  a.pos = d_pos;
+  a.W = W;
+  a.move = o->move;
+  a.step = o->step;
+  a.n_eq = o->n_eq;
+  a.n_steps = o->n_steps;
+  a.block_size = o->block_size;
+  a.refresh = o->refresh;
+  a.seed = seed;
+  a.step0 = (uint32_t)step0;
+  a.partials = partials;
+  a.tb_partials = tb_partials;
+  a.status = status;
+  if (mixed) CUDA_TRY(f32(s->sp32, a, grid, st));
+  else CUDA_TRY(f64(s->sp64, a, grid, st));
+  CUDA_TRY(launch_reduce_columns(partials, grid, NA, reduced, st));
+  if (n_tb > 0) CUDA_TRY(launch_reduce_columns(tb_partials, grid, n_tb, d_time_blocks, st));
+  CUDA_TRY(launch_unpack_vmc_sums(reduced, PM, P, d_moments, o->sr ? d_sr : nullptr, st));
+  int h_status = 0;
+  CUDA_TRY(cudaMemcpyAsync(&h_status, status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  if (h_status & 2) return fail(MOLE_ERR_LINALG, "singular Slater matrix encountered");
+  if (h_status & 1) return fail(MOLE_ERR_FUNC, "non-finite local energy encountered");
+  return MOLE_OK;
 }
 
 int mole_sr_update(mole_ctx* ctx, int32_t P, double count, const double* sum_E, const double* sum_O,

@@ -48,6 +48,23 @@ __global__ void reduce_columns_kernel(const double* part, int rows, int cols, do
   out[c] = s;
 }
 
+__global__ void unpack_vmc_sums_kernel(const double* red, int PM, int P, double* moments, double* sr) {
+  const int t = threadIdx.x;
+  if (t < 7) moments[t] = red[t];
+  if (!sr) return;
+  for (int p = t; p < P; p += blockDim.x) {
+    sr[p] = red[7 + p];
+    sr[P + p] = red[7 + PM + p];
+  }
+  int q = 7 + 2 * PM;
+  for (int p = 0; p < PM; ++p)
+    for (int r = p; r < PM; ++r, ++q)
+      if (t == 0 && p < P && r < P) {
+        sr[2 * P + p * P + r] = red[q];
+        sr[2 * P + r * P + p] = red[q];
+      }
+}
+
 // ---------------------------------------------------------------- DMC comb
 
 // Per-CTA inclusive scan of the weights; CTA totals to btot.
@@ -171,6 +188,10 @@ cudaError_t launch_soa_to_aos(const double* soa, double* aos, int W, int NC, cud
 }
 cudaError_t launch_reduce_columns(const double* part, int rows, int cols, double* out, cudaStream_t s) {
   reduce_columns_kernel<<<(cols + 127) / 128, 128, 0, s>>>(part, rows, cols, out);
+  return cudaGetLastError();
+}
+cudaError_t launch_unpack_vmc_sums(const double* red, int PM, int P, double* moments, double* sr, cudaStream_t s) {
+  unpack_vmc_sums_kernel<<<1, 32, 0, s>>>(red, PM, P, moments, sr);
   return cudaGetLastError();
 }
 cudaError_t launch_comb(const double* weight, double* cum, double* btot, int nb, const double* partials, int n_part,

@@ -18,6 +18,10 @@ cudaError_t launch_init_positions(double* pos, int W, int N, uint64_t seed, int 
 cudaError_t launch_aos_to_soa(const double* aos, double* soa, int W, int NC, cudaStream_t s);
 cudaError_t launch_soa_to_aos(const double* soa, double* aos, int W, int NC, cudaStream_t s);
 cudaError_t launch_reduce_columns(const double* part, int rows, int cols, double* out, cudaStream_t s);
+// Reduced VMC sums (7 moments, then PM O sums, PM E*O sums, upper triangle of
+// O O^T) -> moments[7] and, if sr is not NULL, sr = [sum_O (P), sum_EO (P),
+// sum_OO (P x P)].
+cudaError_t launch_unpack_vmc_sums(const double* red, int PM, int P, double* moments, double* sr, cudaStream_t s);
 cudaError_t launch_comb(const double* weight, double* cum, double* btot, int nb, const double* partials, int n_part,
                         CombState* cs, uint64_t* step, uint64_t seed, double* energies, int64_t e_index,
                         const double* pos_in, const double* eloc_in, double* pos_out, double* eloc_out, int W, int NC,
