@@ -232,6 +232,26 @@ int mole_sr_update(mole_ctx* ctx, int32_t P, double count, const double* sum_E, 
                    const double* sum_EO, const double* sum_OO, double eps, double step, double* delta,
                    double* grad);
 
+/* Stochastic reconfiguration for thousands of parameters (the neural Jastrow):
+ * replaces StochasticReconfiguration::construct_sr_matrix and the solveh call
+ * (src/optimize/src/optimizers.rs:191-252) when P is too large for per-walker
+ * sums. Each sample takes O_k = d ln psi / d theta_k and E_L of every walker at
+ * its current position (move the walkers with mole_vmc_run in between), centres
+ * O on the first sample's mean c, and accumulates S = sum (O-c)(O-c)^T on the
+ * tensor cores (BF16 operands, FP32 accumulation inside a 128 x 128 tile, FP64
+ * across tiles and samples). mole_sr_collect_solve forms
+ * S_kl = <(O-c)_k (O-c)_l> - <O-c>_k <O-c>_l + eps delta_kl and
+ * g_k = 2 (<E O_k> - <E><O_k>) and solves S x = -g/2 in FP64 by
+ * Jacobi-preconditioned conjugate gradients (max_iter, relative residual tol;
+ * 0 picks 500 and 1e-8); delta = step x. info[4] = {mean E, samples, CG
+ * iterations, relative residual}. MOLE_ERR_LINALG when CG does not converge. */
+int mole_sr_collect_begin(mole_walkers* w);
+int mole_sr_collect_sample(mole_walkers* w, int32_t precision);
+int mole_sr_collect_solve(mole_walkers* w, double eps, double step, int32_t max_iter, double tol, double* delta,
+                          double* grad, double* info);
+/* The finalised S matrix (P x P, row-major) of the collected samples. */
+int mole_sr_collect_matrix(mole_walkers* w, double eps, double* S);
+
 /* ---------------------------------------------------------------------- DMC */
 /* DmcRunner::diffuse inner loop (src/dmc/src/dmc.rs:81-141) for opts->n_steps
  * steps: drift-diffusion sweep with Metropolis accept/reject, weight

@@ -88,6 +88,10 @@ SIGNATURES = {
     "mole_vmc_run_noalloc": (C.c_int, [_P, C.c_void_p, C.c_int32, C.c_uint64, C.c_uint64, C.POINTER(VmcOpts),
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mole_sr_update": (C.c_int, [_P, C.c_int32, C.c_double, _D, _D, _D, _D, C.c_double, C.c_double, _D, _D]),
+    "mole_sr_collect_begin": (C.c_int, [_P]),
+    "mole_sr_collect_sample": (C.c_int, [_P, C.c_int32]),
+    "mole_sr_collect_solve": (C.c_int, [_P, C.c_double, C.c_double, C.c_int32, C.c_double, _D, _D, _D]),
+    "mole_sr_collect_matrix": (C.c_int, [_P, C.c_double, _D]),
     "mole_dmc_run": (C.c_int, [_P, C.POINTER(DmcOpts), _D, _D]),
     "mole_checkpoint_save": (C.c_int, [_P, C.c_char_p]),
     "mole_checkpoint_load": (C.c_int, [_P, C.c_char_p]),

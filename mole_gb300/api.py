@@ -199,6 +199,25 @@ class Walkers:
                                  dptr(r["lap"]), dptr(r["eloc"]), dptr(r["O"])))
         return r
 
+    # --- stochastic reconfiguration with many parameters (the neural Jastrow)
+    def sr_collect_begin(self):
+        check(self.lib.mole_sr_collect_begin(self.h))
+
+    def sr_collect_sample(self, precision: int = PREC_MIXED):
+        check(self.lib.mole_sr_collect_sample(self.h, precision))
+
+    def sr_collect_solve(self, eps: float, step: float, max_iter: int = 500, tol: float = 1e-8):
+        P = self.wf.num_parameters()
+        delta, g, info = np.zeros(P), np.zeros(P), np.zeros(4)
+        check(self.lib.mole_sr_collect_solve(self.h, eps, step, max_iter, tol, dptr(delta), dptr(g), dptr(info)))
+        return delta, g, info
+
+    def sr_collect_matrix(self, eps: float) -> np.ndarray:
+        P = self.wf.num_parameters()
+        S = np.zeros((P, P))
+        check(self.lib.mole_sr_collect_matrix(self.h, eps, dptr(S)))
+        return S
+
     def save(self, path: str):
         check(self.lib.mole_checkpoint_save(self.h, path.encode()))
 
@@ -410,10 +429,27 @@ class OnlineLbfgs:
 
 class StochasticReconfiguration:
     """optimizers.rs:194-265 with O_k = d ln psi / d p_k, S_kl = <O_k O_l> - <O_k><O_l>,
-    S_kk += eps and delta = step * S^-1 (-g/2), solved in FP64 on the device side."""
+    S_kk += eps and delta = step * S^-1 (-g/2), solved in FP64 on the device side.
+    With more than 8 parameters (the neural Jastrow) the sums are not
+    accumulated per walker: VmcRunner takes `samples` O_k samples of the whole
+    ensemble per iteration, `sample_every` sweeps apart, and S is built on the
+    tensor cores and solved by conjugate gradients."""
 
-    def __init__(self, step_size: float, eps: float = 1e-3):
+    def __init__(self, step_size: float, eps: float = 1e-3, samples: int = 8, sample_every: int = 10,
+                 precision: int = PREC_MIXED):
         self.step_size, self.eps = step_size, eps
+        self.samples, self.sample_every, self.precision = samples, sample_every, precision
+        self.last_info = None
+
+    def collect_and_solve(self, sampler: "Sampler"):
+        wk = sampler.walkers
+        wk.sr_collect_begin()
+        for _ in range(self.samples):
+            sampler.run(0, self.sample_every, self.sample_every)
+            wk.sr_collect_sample(self.precision)
+        delta, g, info = wk.sr_collect_solve(self.eps, self.step_size)
+        self.last_info = info
+        return delta, g
 
     def compute_parameter_update(self, pars, result: MonteCarloResult, ctx: Context):
         P = result.sum_O.size
@@ -438,12 +474,18 @@ class VmcRunner:
     def run_optimization(self, iters: int, steps: int, block_size: int, callback=None):
         wf = self.sampler.wave_function()
         energies, errors, results = [], [], []
+        large = wf.num_parameters() > 8
         for it in range(iters):
-            r = Runner(self.sampler).run(steps, block_size, sr=True)
+            r = Runner(self.sampler).run(steps, block_size, sr=not large)
             energies.append(r.energy)
             errors.append(r.error)
             results.append(r)
-            delta = self.optimizer.compute_parameter_update(wf.parameters(), r, wf.ctx)
+            if large:
+                if not isinstance(self.optimizer, StochasticReconfiguration):
+                    raise MoleError(103, "only StochasticReconfiguration handles more than 8 parameters")
+                delta, _ = self.optimizer.collect_and_solve(self.sampler)
+            else:
+                delta = self.optimizer.compute_parameter_update(wf.parameters(), r, wf.ctx)
             wf.update_parameters(delta)
             if callback:
                 callback(it, r, wf)

@@ -10,6 +10,7 @@
 #include "../../include/mole_gpu.h"
 #include "dispatch.cuh"
 #include "ensemble.cuh"
+#include "sr_large.cuh"
 
 namespace mole {
 #define MOLE_DECL(NU, ND)                           \
@@ -19,6 +20,8 @@ MOLE_DECL(1, 0)
 MOLE_DECL(1, 1)
 MOLE_DECL(2, 1)
 MOLE_DECL(2, 2)
+const NnKernelSetT<double>* nn_kernels_f64_2_2();
+const NnKernelSetT<float>* nn_kernels_f32_2_2();
 
 #define MOLE_CASE(NU, ND, TAG) \
   if (nu == NU && nd == ND) return kernels_##TAG##_##NU##_##ND();
@@ -98,6 +101,9 @@ struct mole_system {
   SysParams<float> sp32;
   const KernelSetT<double>* k64 = nullptr;
   const KernelSetT<float>* k32 = nullptr;
+  const NnKernelSetT<double>* nk64 = nullptr;  // neural systems
+  const NnKernelSetT<float>* nk32 = nullptr;
+  double* d_nn_theta = nullptr;  // device copy of the network parameters
   int refs = 1;
   bool closed = false;
 };
@@ -115,6 +121,10 @@ struct mole_walkers {
   uint64_t* dstep = nullptr;
   CombState* comb = nullptr;
   bool eloc_valid = false;
+  // many-parameter SR (allocated on first use)
+  SrLargeState* srl = nullptr;
+  CUtensorMap* srl_map = nullptr;
+  double* srl_eval = nullptr;  // eval outputs: lnpsi, sign, lap, grad, O[W][8]
 };
 
 namespace {
@@ -177,14 +187,37 @@ void fill_params(const mole_system& s, SysParams<R>& sp) {
       vnn += (double)(s.nuc_z[I] * s.nuc_z[K]) / std::sqrt(d2);
     }
   sp.vnn = vnn;
+  sp.nn_theta = s.d_nn_theta;
 }
 
-void rebuild(mole_system& s) {
+// Re-derives both kernel-parameter images and, for neural systems, the
+// device copy of the network parameters (a synchronous 72 KB copy).
+cudaError_t rebuild(mole_system& s) {
   fill_params(s, s.sp64);
   fill_params(s, s.sp32);
+  if (s.nn_on && s.d_nn_theta) {
+    const int off = s.n_exp + (s.ee_on ? 1 + s.ee_npoly : 0) + (s.en_on ? 1 : 0);
+    return cudaMemcpy(s.d_nn_theta, s.theta.data() + off, sizeof(double) * kNnP, cudaMemcpyHostToDevice);
+  }
+  return cudaSuccess;
 }
 
 int grid_for(int W) { return (W + kBlock - 1) / kBlock; }
+
+// Kernel selection: neural systems use the network kernels (no in-kernel SR
+// sums), the others the family's kernels with or without the e-n term.
+KernelSetT<double>::Vmc vmc64(const mole_system* s, int slot, int drift) {
+  if (s->nn_on) return slot == 0 ? s->nk64->vmc[drift] : nullptr;
+  return s->k64->vmc[slot][drift][s->en_on];
+}
+KernelSetT<float>::Vmc vmc32(const mole_system* s, int slot, int drift) {
+  if (s->nn_on) return slot == 0 ? s->nk32->vmc[drift] : nullptr;
+  return s->k32->vmc[slot][drift][s->en_on];
+}
+KernelSetT<double>::Eval eval64(const mole_system* s) { return s->nn_on ? s->nk64->eval : s->k64->eval[s->en_on]; }
+KernelSetT<float>::Eval eval32(const mole_system* s) { return s->nn_on ? s->nk32->eval : s->k32->eval[s->en_on]; }
+KernelSetT<double>::Dmc dmc64(const mole_system* s) { return s->nn_on ? s->nk64->dmc : s->k64->dmc[s->en_on]; }
+KernelSetT<float>::Dmc dmc32(const mole_system* s) { return s->nn_on ? s->nk32->dmc : s->k32->dmc[s->en_on]; }
 
 int check_status(mole_ctx* ctx) {
   int st = 0;
@@ -262,6 +295,11 @@ static void release_ctx(mole_ctx* c) {
 
 static void release_sys(mole_system* s) {
   if (--s->refs > 0) return;
+  if (s->d_nn_theta) {
+    cudaSetDevice(s->ctx->device);
+    cudaFree(s->d_nn_theta);
+    cudaGetLastError();
+  }
   mole_ctx* c = s->ctx;
   delete s;
   release_ctx(c);
@@ -347,7 +385,8 @@ int mole_system_create(mole_ctx* ctx, const mole_system_desc* d, const double* t
   if (!d->nuc_pos || !d->nuc_charge || !d->basis_center || !d->basis_kind || !d->basis_exp || !d->coef_up ||
       (d->n_dn > 0 && !d->coef_dn) || (d->en_on && !d->en_coef))
     return fail(MOLE_ERR_INVALID_ARG, "NULL descriptor array");
-  if (d->nn_on) return fail(MOLE_ERR_UNSUPPORTED, "neural Jastrow systems are created with mole_nn_system_create");
+  if (d->nn_on && !(d->n_up == 2 && d->n_dn == 2))
+    return fail(MOLE_ERR_UNSUPPORTED, "neural-Jastrow kernels are compiled for 2 up + 2 down electrons");
   auto s = new mole_system();
   s->ctx = ctx;
   s->n_nuc = d->n_nuclei;
@@ -377,10 +416,10 @@ int mole_system_create(mole_ctx* ctx, const mole_system_desc* d, const double* t
   s->cusp_anti = d->cusp_anti;
   s->cusp_para = d->cusp_para;
   s->en_on = d->en_on != 0;
-  s->nn_on = 0;
+  s->nn_on = d->nn_on != 0;
   s->pot_kind = d->pot_kind;
   s->omega = d->omega;
-  s->P = s->n_exp + (s->ee_on ? 1 + s->ee_npoly : 0) + (s->en_on ? 1 : 0);
+  s->P = s->n_exp + (s->ee_on ? 1 + s->ee_npoly : 0) + (s->en_on ? 1 : 0) + (s->nn_on ? kNnP : 0);
   if (!theta || n_theta != s->P) {
     const int P = s->P;
     delete s;
@@ -393,7 +432,21 @@ int mole_system_create(mole_ctx* ctx, const mole_system_desc* d, const double* t
     delete s;
     return fail(MOLE_ERR_UNSUPPORTED, "no compiled kernels for this (n_up, n_dn); supported: n_dn = n_up or n_up - 1");
   }
-  rebuild(*s);
+  if (s->nn_on) {
+    s->nk64 = nn_kernels_f64_2_2();
+    s->nk32 = nn_kernels_f32_2_2();
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_nn_theta, sizeof(double) * kNnP);
+    if (e != cudaSuccess) {
+      delete s;
+      return fail(MOLE_ERR_CUDA, std::string("network parameters: ") + cudaGetErrorString(e));
+    }
+  }
+  if (rebuild(*s) != cudaSuccess) {
+    if (s->d_nn_theta) cudaFree(s->d_nn_theta);
+    delete s;
+    return fail(MOLE_ERR_CUDA, "copying the network parameters failed");
+  }
   ctx->refs += 1;
   *out = s;
   return MOLE_OK;
@@ -429,7 +482,7 @@ int mole_params_set(mole_system* s, const double* theta, int32_t n) {
   if (!s || !theta) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
   if (n != s->P) return fail(MOLE_ERR_SHAPE, "parameter count mismatch");
   s->theta.assign(theta, theta + n);
-  rebuild(*s);
+  CUDA_TRY(rebuild(*s));
   return MOLE_OK;
 }
 
@@ -469,6 +522,18 @@ static void free_dmc(mole_walkers* w) {
   w->comb = nullptr;
   w->energies_n = 0;
   w->eloc_valid = false;
+  if (w->srl) {
+    SrLargeState* t = w->srl;
+    for (void* p : {(void*)t->O, (void*)t->Ot, (void*)t->S, (void*)t->E, (void*)t->center, (void*)t->sumO,
+                    (void*)t->sumEO, (void*)t->work, (void*)t->status})
+      if (p) cudaFree(p);
+    delete t;
+    w->srl = nullptr;
+  }
+  delete w->srl_map;
+  w->srl_map = nullptr;
+  if (w->srl_eval) cudaFree(w->srl_eval);
+  w->srl_eval = nullptr;
 }
 
 int mole_walkers_destroy(mole_walkers* w) {
@@ -545,7 +610,10 @@ int mole_eval(mole_walkers* w, int32_t precision, double* lnpsi, double* sign, d
   mole_system* s = w->sys;
   mole_ctx* c = s->ctx;
   const int W = w->W, N = s->n_up + s->n_dn, P = s->P;
-  if (P > 8 && O) return fail(MOLE_ERR_UNSUPPORTED, "O_k output supports at most 8 parameters here");
+  const int nwalker_par = s->nn_on ? P - kNnP : P;
+  if (nwalker_par > 8 && O) return fail(MOLE_ERR_UNSUPPORTED, "O_k output supports at most 8 orbital/Pade parameters");
+  if (s->nn_on && O && (N * (N - 1) / 2 > 8 || N * s->n_nuc > 8))
+    return fail(MOLE_ERR_UNSUPPORTED, "network O_k supports at most 8 pairs per network");
   const size_t per = 5 + 3 * (size_t)N + P;
   CUDA_TRY(c->reduced.reserve(per * W));
   double* base = c->reduced.p;
@@ -558,11 +626,15 @@ int mole_eval(mole_walkers* w, int32_t precision, double* lnpsi, double* sign, d
   a.eloc = base + 3 * (size_t)W;
   a.grad = base + 4 * (size_t)W;
   a.O = a.grad + 3 * (size_t)N * W;
+  a.ldO = P;
   CUDA_TRY(cudaMemsetAsync(c->status.p, 0, sizeof(int), c->stream));
   a.status = c->status.p;
   Timer tm(c, 2);
-  if (precision == MOLE_PREC_MIXED) CUDA_TRY(s->k32->eval[s->en_on](s->sp32, a, grid_for(W), c->stream));
-  else CUDA_TRY(s->k64->eval[s->en_on](s->sp64, a, grid_for(W), c->stream));
+  if (precision == MOLE_PREC_MIXED) CUDA_TRY(eval32(s)(s->sp32, a, grid_for(W), c->stream));
+  else CUDA_TRY(eval64(s)(s->sp64, a, grid_for(W), c->stream));
+  if (s->nn_on && O)  // the network's O_k (FP32 arithmetic) after the orbital/Pade ones
+    CUDA_TRY(launch_nn_ogen64(s->sp32, w->pos, W, s->n_up, N, a.O, P, nwalker_par, std::min(W, 3 * c->n_sm),
+                              c->stream));
   tm.stop();
   auto copy = [&](double* dst, const double* src, size_t n) -> int {
     if (dst) CUDA_TRY(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
@@ -602,8 +674,8 @@ int mole_vmc_run(mole_walkers* w, const mole_vmc_opts* o, double* moments, doubl
   const int PM = kPmWidth[slot];
   const int drift = o->move == MOLE_MOVE_DIFFUSE ? 1 : 0;
   const bool mixed = o->precision == MOLE_PREC_MIXED;
-  auto f64 = s->k64->vmc[slot][drift][s->en_on];
-  auto f32 = s->k32->vmc[slot][drift][s->en_on];
+  auto f64 = vmc64(s, slot, drift);
+  auto f32 = vmc32(s, slot, drift);
   if (mixed ? !f32 : !f64) return fail(MOLE_ERR_UNSUPPORTED, "SR kernel not compiled for this family and precision");
   const int W = w->W, grid = grid_for(W), NA = n_acc(PM);
   const int n_tb = o->n_steps / o->block_size;
@@ -706,8 +778,8 @@ int mole_vmc_run_noalloc(const mole_system* s, double* d_pos, int32_t W, uint64_
   }
   const int PM = kPmWidth[slot];
   const int drift = o->move == MOLE_MOVE_DIFFUSE ? 1 : 0;
-  auto f64 = s->k64->vmc[slot][drift][s->en_on];
-  auto f32 = s->k32->vmc[slot][drift][s->en_on];
+  auto f64 = vmc64(s, slot, drift);
+  auto f32 = vmc32(s, slot, drift);
   if (mixed ? !f32 : !f64) return fail(MOLE_ERR_UNSUPPORTED, "kernel not compiled for this family and precision");
   const int grid = grid_for(W), NA = n_acc(PM), n_tb = o->n_steps / o->block_size;
   // scratch layout: partials [grid][NA] | time-block partials [grid][n_tb] | reduced [NA] | status
@@ -751,6 +823,167 @@ int mole_vmc_run_noalloc(const mole_system* s, double* d_pos, int32_t W, uint64_
   CUDA_TRY(cudaStreamSynchronize(st));
   if (h_status & 2) return fail(MOLE_ERR_LINALG, "singular Slater matrix encountered");
   if (h_status & 1) return fail(MOLE_ERR_FUNC, "non-finite local energy encountered");
+  return MOLE_OK;
+}
+
+int mole_sr_collect_begin(mole_walkers* w) {
+  if (!w) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
+  cudaGetLastError();  // report only errors raised by this call
+  mole_system* s = w->sys;
+  mole_ctx* c = s->ctx;
+  CUDA_TRY(cudaSetDevice(c->device));
+  const int W = w->W, P = s->P;
+  if (!w->srl) {
+    auto t = new SrLargeState();
+    std::memset(t, 0, sizeof(*t));
+    t->P = P;
+    t->P_pad = (P + kSBM - 1) / kSBM * kSBM;
+    t->K_pad = (W + kSBK - 1) / kSBK * kSBK;
+    w->srl = t;  // freed by free_dmc on failure below
+    CUDA_TRY(cudaMalloc(&t->O, sizeof(float) * (size_t)W * P));
+    CUDA_TRY(cudaMalloc(&t->Ot, sizeof(__nv_bfloat16) * (size_t)t->P_pad * t->K_pad));
+    CUDA_TRY(cudaMemset(t->Ot, 0, sizeof(__nv_bfloat16) * (size_t)t->P_pad * t->K_pad));  // zero padding
+    CUDA_TRY(cudaMalloc(&t->S, sizeof(double) * (size_t)t->P_pad * t->P_pad));
+    CUDA_TRY(cudaMalloc(&t->E, sizeof(double) * W));
+    CUDA_TRY(cudaMalloc(&t->center, sizeof(double) * P));
+    CUDA_TRY(cudaMalloc(&t->sumO, sizeof(double) * P));
+    CUDA_TRY(cudaMalloc(&t->sumEO, sizeof(double) * P));
+    CUDA_TRY(cudaMalloc(&t->work, sizeof(double) * (6 * (size_t)P + 8)));
+    CUDA_TRY(cudaMalloc(&t->status, sizeof(int)));
+    CUDA_TRY(cudaMalloc(&w->srl_eval, sizeof(double) * (size_t)W * (3 + 3 * (s->n_up + s->n_dn) + 8)));
+    w->srl_map = new CUtensorMap();
+    CUDA_TRY(encode_ot_tensor_map(w->srl_map, t->Ot, t->P_pad, t->K_pad));
+  }
+  SrLargeState* t = w->srl;
+  CUDA_TRY(cudaMemsetAsync(t->S, 0, sizeof(double) * (size_t)t->P_pad * t->P_pad, c->stream));
+  CUDA_TRY(cudaMemsetAsync(t->sumO, 0, sizeof(double) * P, c->stream));
+  CUDA_TRY(cudaMemsetAsync(t->sumEO, 0, sizeof(double) * P, c->stream));
+  CUDA_TRY(cudaMemsetAsync(t->status, 0, sizeof(int), c->stream));
+  t->count = 0.0;
+  t->sumE = t->sumE2 = 0.0;
+  t->have_center = false;
+  t->finalized = false;
+  return MOLE_OK;
+}
+
+static int srl_finalize(mole_walkers* w, double eps) {
+  SrLargeState* t = w->srl;
+  mole_ctx* c = w->sys->ctx;
+  if (t->finalized) {
+    if (eps != t->eps) return fail(MOLE_ERR_INVALID_ARG, "S was already finalised with another shift");
+    return MOLE_OK;
+  }
+  CUDA_TRY(launch_finalize_s(t->S, t->P, t->P_pad, t->sumO, t->count, eps, c->stream));
+  t->finalized = true;
+  t->eps = eps;
+  return MOLE_OK;
+}
+
+int mole_sr_collect_matrix(mole_walkers* w, double eps, double* S_out) {
+  if (!w || !S_out) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
+  if (!w->srl || !(w->srl->count > 0)) return fail(MOLE_ERR_EMPTY_CACHE, "no samples collected");
+  cudaGetLastError();  // report only errors raised by this call
+  SrLargeState* t = w->srl;
+  mole_ctx* c = w->sys->ctx;
+  const int rc = srl_finalize(w, eps);
+  if (rc) return rc;
+  CUDA_TRY(cudaMemcpy2DAsync(S_out, sizeof(double) * t->P, t->S, sizeof(double) * t->P_pad, sizeof(double) * t->P,
+                             t->P, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return MOLE_OK;
+}
+
+int mole_sr_collect_sample(mole_walkers* w, int32_t precision) {
+  if (!w || !w->srl) return fail(MOLE_ERR_EMPTY_CACHE, "call mole_sr_collect_begin first");
+  cudaGetLastError();  // report only errors raised by this call
+  mole_system* s = w->sys;
+  mole_ctx* c = s->ctx;
+  SrLargeState* t = w->srl;
+  if (t->finalized) return fail(MOLE_ERR_EMPTY_CACHE, "S was finalised; call mole_sr_collect_begin again");
+  const int W = w->W, N = s->n_up + s->n_dn, P = s->P;
+  const int nwalker_par = s->nn_on ? P - kNnP : P;
+  if (nwalker_par > 8) return fail(MOLE_ERR_UNSUPPORTED, "more than 8 orbital/Pade parameters");
+  if (s->nn_on && (N * (N - 1) / 2 > 8 || N * s->n_nuc > 8))
+    return fail(MOLE_ERR_UNSUPPORTED, "network O_k supports at most 8 pairs per network");
+  CUDA_TRY(cudaMemsetAsync(c->status.p, 0, sizeof(int), c->stream));
+  // E_L and the orbital/Pade O_k at the current positions
+  EvalArgs a;
+  a.pos = w->pos;
+  a.W = W;
+  a.lnpsi = w->srl_eval;
+  a.sign = a.lnpsi + W;
+  a.lap = a.sign + W;
+  a.grad = a.lap + W;
+  a.O = a.grad + (size_t)3 * N * W;
+  a.ldO = 8;
+  a.eloc = t->E;
+  a.status = c->status.p;
+  Timer tm(c, 2);
+  if (precision == MOLE_PREC_MIXED) CUDA_TRY(eval32(s)(s->sp32, a, grid_for(W), c->stream));
+  else CUDA_TRY(eval64(s)(s->sp64, a, grid_for(W), c->stream));
+  CUDA_TRY(launch_copy_cols(a.O, 8, nwalker_par, t->O, P, W, c->stream));
+  if (s->nn_on)
+    CUDA_TRY(launch_nn_ogen(s->sp32, w->pos, W, s->n_up, N, t->O, P, nwalker_par, std::min(W, 3 * c->n_sm),
+                            c->stream));
+  CUDA_TRY(launch_center_transpose(t->O, W, P, P, t->E, t->center, !t->have_center, t->Ot, t->K_pad, t->sumO,
+                                   t->sumEO, nullptr, c->stream));
+  t->have_center = true;
+  CUDA_TRY(launch_s_gemm(w->srl_map, t->S, t->P_pad, t->K_pad, t->status, c->stream));
+  tm.stop();
+  std::vector<double> e(W);
+  CUDA_TRY(cudaMemcpyAsync(e.data(), t->E, sizeof(double) * W, cudaMemcpyDeviceToHost, c->stream));
+  int st = 0;
+  CUDA_TRY(cudaMemcpyAsync(&st, t->status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (st & 4) return fail(MOLE_ERR_TIMEOUT, "S-matrix kernel wait timed out");
+  for (double v : e) {
+    t->sumE += v;
+    t->sumE2 += v * v;
+  }
+  t->count += W;
+  return check_status(c);
+}
+
+int mole_sr_collect_solve(mole_walkers* w, double eps, double step, int32_t max_iter, double tol, double* delta,
+                          double* grad, double* info) {
+  if (!w || !delta) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
+  if (!w->srl || !(w->srl->count > 0)) return fail(MOLE_ERR_EMPTY_CACHE, "no samples collected");
+  cudaGetLastError();  // report only errors raised by this call
+  mole_system* s = w->sys;
+  mole_ctx* c = s->ctx;
+  SrLargeState* t = w->srl;
+  const int P = s->P;
+  const double n = t->count, Eb = t->sumE / n;
+  std::vector<double> sO(P), sEO(P), b(P), x(P);
+  CUDA_TRY(cudaMemcpyAsync(sO.data(), t->sumO, sizeof(double) * P, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(sEO.data(), t->sumEO, sizeof(double) * P, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  // g_k = 2 (<E O_k> - <E><O_k>), centring-invariant; b = -g / 2
+  for (int k = 0; k < P; ++k) {
+    const double g = 2.0 * (sEO[k] / n - Eb * sO[k] / n);
+    if (grad) grad[k] = g;
+    b[k] = -0.5 * g;
+  }
+  const int frc = srl_finalize(w, eps);
+  if (frc) return frc;
+  double* d_b = t->work + 5 * (size_t)P + 8;  // scratch after the CG vectors
+  double* d_x = t->center;                     // reuse: the centre is not needed after the last sample
+  CUDA_TRY(cudaMemcpyAsync(d_b, b.data(), sizeof(double) * P, cudaMemcpyHostToDevice, c->stream));
+  int iters = 0;
+  double rel = 0.0;
+  CUDA_TRY(sr_cg_solve(t->S, P, t->P_pad, d_b, d_x, t->work, max_iter > 0 ? max_iter : 500, tol > 0 ? tol : 1e-8,
+                       &iters, &rel, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(x.data(), d_x, sizeof(double) * P, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < P; ++k) delta[k] = step * x[k];
+  if (info) {
+    info[0] = Eb;
+    info[1] = n;
+    info[2] = iters;
+    info[3] = rel;
+  }
+  t->have_center = false;
+  if (!(rel < 1e-3)) return fail(MOLE_ERR_LINALG, "CG did not converge on the SR system");
   return MOLE_OK;
 }
 
@@ -827,7 +1060,7 @@ int mole_dmc_run(mole_walkers* w, const mole_dmc_opts* o, double* energies, doub
   mole_system* s = w->sys;
   mole_ctx* c = s->ctx;
   const bool mixed = o->precision == MOLE_PREC_MIXED;
-  if (mixed ? !s->k32->dmc[s->en_on] : !s->k64->dmc[s->en_on])
+  if (mixed ? !dmc32(s) : !dmc64(s))
     return fail(MOLE_ERR_UNSUPPORTED, "DMC kernels are compiled for up to four electrons");
   const int W = w->W, NC = 3 * (s->n_up + s->n_dn), grid = grid_for(W);
   const int nb = (W + kScanBlock - 1) / kScanBlock;
@@ -846,14 +1079,11 @@ int mole_dmc_run(mole_walkers* w, const mole_dmc_opts* o, double* energies, doub
     a.lap = a.sign + W;
     a.eloc = w->eloc;
     a.grad = a.lap + W;
-    a.O = nullptr;
+    a.O = nullptr;  // no parameter derivatives needed
+    a.ldO = 0;
     a.status = c->status.p;
-    if (s->P > 0) {
-      CUDA_TRY(c->scratch.reserve((size_t)s->P * W));
-      a.O = c->scratch.p;
-    }
-    if (mixed) CUDA_TRY(s->k32->eval[s->en_on](s->sp32, a, grid, c->stream));
-    else CUDA_TRY(s->k64->eval[s->en_on](s->sp64, a, grid, c->stream));
+    if (mixed) CUDA_TRY(eval32(s)(s->sp32, a, grid, c->stream));
+    else CUDA_TRY(eval64(s)(s->sp64, a, grid, c->stream));
     w->eloc_valid = true;
   }
   const uint64_t step = w->step;
@@ -874,8 +1104,8 @@ int mole_dmc_run(mole_walkers* w, const mole_dmc_opts* o, double* energies, doub
   for (int t = 0; t < o->n_steps; ++t) {
     a.pos = w->pos;
     a.eloc = w->eloc;
-    if (mixed) CUDA_TRY(s->k32->dmc[s->en_on](s->sp32, a, grid, c->stream));
-    else CUDA_TRY(s->k64->dmc[s->en_on](s->sp64, a, grid, c->stream));
+    if (mixed) CUDA_TRY(dmc32(s)(s->sp32, a, grid, c->stream));
+    else CUDA_TRY(dmc64(s)(s->sp64, a, grid, c->stream));
     CUDA_TRY(launch_comb(w->weight, w->cum, w->btot, nb, c->partials.p, grid, w->comb, w->dstep, w->seed,
                          w->energies, t, w->pos, w->eloc, w->pos2, w->eloc2, W, NC, c->stream));
     std::swap(w->pos, w->pos2);

@@ -64,4 +64,52 @@ typename KernelSetT<R>::Dmc maybe_dmc() {
 const KernelSetT<double>* kernel_set64(int nu, int nd);
 const KernelSetT<float>* kernel_set32(int nu, int nd);
 
+// Neural-Jastrow kernels (e-n terms on; the weights in dynamic shared memory).
+template <class R>
+struct NnKernelSetT {
+  typename KernelSetT<R>::Vmc vmc[2];  // [drift]
+  typename KernelSetT<R>::Eval eval;
+  typename KernelSetT<R>::Dmc dmc;
+};
+
+template <class K>
+cudaError_t nn_prepare(K kernel, size_t smem) {
+  // opt in to more than 48 KB of dynamic shared memory (idempotent)
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+template <int NU, int ND, class R, bool DRIFT>
+cudaError_t launch_vmc_nn(const SysParams<R>& sp, const VmcArgs& a, int grid, cudaStream_t s) {
+  auto k = vmc_kernel<NU, ND, R, 0, DRIFT, true, true>;
+  const size_t smem = nn_smem_bytes<R>(kBlock);
+  cudaError_t e = nn_prepare(k, smem);
+  if (e != cudaSuccess) return e;
+  k<<<grid, kBlock, smem, s>>>(sp, a);
+  return cudaGetLastError();
+}
+template <int NU, int ND, class R>
+cudaError_t launch_eval_nn(const SysParams<R>& sp, const EvalArgs& a, int grid, cudaStream_t s) {
+  auto k = eval_kernel<NU, ND, R, 8, true, true>;
+  const size_t smem = nn_smem_bytes<R>(kBlock);
+  cudaError_t e = nn_prepare(k, smem);
+  if (e != cudaSuccess) return e;
+  k<<<grid, kBlock, smem, s>>>(sp, a);
+  return cudaGetLastError();
+}
+template <int NU, int ND, class R>
+cudaError_t launch_dmc_nn(const SysParams<R>& sp, const DmcArgs& a, int grid, cudaStream_t s) {
+  auto k = dmc_step_kernel<NU, ND, R, true, true>;
+  const size_t smem = nn_smem_bytes<R>(kBlock);
+  cudaError_t e = nn_prepare(k, smem);
+  if (e != cudaSuccess) return e;
+  k<<<grid, kBlock, smem, s>>>(sp, a);
+  return cudaGetLastError();
+}
+
+#define MOLE_INSTANTIATE_NN(NU, ND, R, TAG)                                                               \
+  const NnKernelSetT<R>* nn_kernels_##TAG##_##NU##_##ND() {                                              \
+    static const NnKernelSetT<R> ks = {{launch_vmc_nn<NU, ND, R, false>, launch_vmc_nn<NU, ND, R, true>}, \
+                                       launch_eval_nn<NU, ND, R>, launch_dmc_nn<NU, ND, R>};             \
+    return &ks;                                                                                          \
+  }
+
 }  // namespace mole

@@ -34,15 +34,32 @@ struct VmcArgs {
 // The energy sums live in registers; the SR sums, touched once per sweep,
 // live in per-thread shared-memory slots srs[k * blockDim.x + tid] to keep
 // the walker caches in registers.
-template <int NU, int ND, class R, int PM, bool EN, int MOVE>
+extern __shared__ __align__(16) unsigned char mole_dyn_smem[];
+
+// Neural systems: loads both networks into the CTA's dynamic shared memory
+// (all threads must call this) and returns this thread's context.
+template <class R, bool NN>
+__device__ __forceinline__ NnCtx<R> nn_setup(const SysParams<R>& sp) {
+  NnCtx<R> c{nullptr, nullptr, 0};
+  if constexpr (NN) {
+    auto* sh = reinterpret_cast<NnShared<R>*>(mole_dyn_smem);
+    nn_load<R>(sh, sp.nn_theta);
+    R* scr = reinterpret_cast<R*>(mole_dyn_smem + sizeof(NnShared<R>));
+    c = NnCtx<R>{sh, scr + threadIdx.x, (int)blockDim.x};
+  }
+  return c;
+}
+
+template <int NU, int ND, class R, int PM, bool EN, bool NN, int MOVE>
 __device__ __forceinline__ void vmc_body(const SysParams<R>& sp, const VmcArgs& a, double* red, double* srs) {
-  using Wk = Walker<NU, ND, R, PM, EN>;
+  using Wk = Walker<NU, ND, R, PM, EN, NN>;
   constexpr int NA = n_acc(PM);
   constexpr int NSR = NA - kNMom;
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
   const int tid = threadIdx.x;
   const bool active = w < a.W;
   Wk wk;
+  wk.nn = nn_setup<R, NN>(sp);
   if (active) wk.load(a.pos, a.W, w);
   else
 #pragma unroll
@@ -109,16 +126,16 @@ __device__ __forceinline__ void vmc_body(const SysParams<R>& sp, const VmcArgs& 
 
 // DRIFT selects the drift-diffusion kernel; otherwise box and Gaussian moves
 // share one kernel (uniform branch on a.move).
-template <int NU, int ND, class R, int PM, bool DRIFT, bool EN>
+template <int NU, int ND, class R, int PM, bool DRIFT, bool EN, bool NN = false>
 __global__ void __launch_bounds__(kBlock, (min_blocks<NU, ND>())) vmc_kernel(const __grid_constant__ SysParams<R> sp,
                                                                             const VmcArgs a) {
   __shared__ double red[kBlock / 32];
   __shared__ double srs[(n_acc(PM) - kNMom > 0 ? n_acc(PM) - kNMom : 1) * kBlock];
   if constexpr (DRIFT) {
-    vmc_body<NU, ND, R, PM, EN, kMoveDiffuse>(sp, a, red, srs);
+    vmc_body<NU, ND, R, PM, EN, NN, kMoveDiffuse>(sp, a, red, srs);
   } else {
-    if (a.move == kMoveBox) vmc_body<NU, ND, R, PM, EN, kMoveBox>(sp, a, red, srs);
-    else vmc_body<NU, ND, R, PM, EN, kMoveGauss>(sp, a, red, srs);
+    if (a.move == kMoveBox) vmc_body<NU, ND, R, PM, EN, NN, kMoveBox>(sp, a, red, srs);
+    else vmc_body<NU, ND, R, PM, EN, NN, kMoveGauss>(sp, a, red, srs);
   }
 }
 
@@ -130,16 +147,18 @@ struct EvalArgs {
   double* grad;       // [W][N][3]
   double* lap;        // [W]
   double* eloc;       // [W]
-  double* O;          // [W][P] (first min(P, PM) entries)
+  double* O;          // [W][ldO] (first min(P, PM, ldO) entries)
+  int ldO;
   int* status;
 };
 
-template <int NU, int ND, class R, int PM, bool EN>
+template <int NU, int ND, class R, int PM, bool EN, bool NN = false>
 __global__ void __launch_bounds__(kBlock) eval_kernel(const __grid_constant__ SysParams<R> sp, const EvalArgs a) {
-  using Wk = Walker<NU, ND, R, PM, EN>;
+  using Wk = Walker<NU, ND, R, PM, EN, NN>;
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
-  if (w >= a.W) return;
   Wk wk;
+  wk.nn = nn_setup<R, NN>(sp);
+  if (w >= a.W) return;
   wk.load(a.pos, a.W, w);
   double ln, sg;
   const bool ok = wk.refresh(sp, &ln, &sg);
@@ -156,7 +175,8 @@ __global__ void __launch_bounds__(kBlock) eval_kernel(const __grid_constant__ Sy
 #pragma unroll
   for (int k = 0; k < Wk::N * 3; ++k) a.grad[(size_t)w * Wk::N * 3 + k] = g[k];
   if constexpr (PM > 0)
-    for (int p = 0; p < sp.P && p < PM; ++p) a.O[(size_t)w * sp.P + p] = O[p];
+    if (a.O)
+      for (int p = 0; p < sp.P && p < PM && p < a.ldO; ++p) a.O[(size_t)w * a.ldO + p] = O[p];
 }
 
 struct DmcArgs {
@@ -172,16 +192,18 @@ struct DmcArgs {
   int* status;
 };
 
-template <int NU, int ND, class R, bool EN>
+template <int NU, int ND, class R, bool EN, bool NN = false>
 __global__ void __launch_bounds__(kBlock, (min_blocks<NU, ND>())) dmc_step_kernel(const __grid_constant__ SysParams<R> sp, const DmcArgs a) {
-  using Wk = Walker<NU, ND, R, 0, EN>;
+  using Wk = Walker<NU, ND, R, 0, EN, NN>;
   __shared__ double red[3 * kBlock / 32];
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = w < a.W;
   const uint32_t t = (uint32_t)(*a.step);
   double v[3] = {0.0, 0.0, 0.0};
+  const NnCtx<R> nnc = nn_setup<R, NN>(sp);
   if (active) {
     Wk wk;
+    wk.nn = nnc;
     wk.load(a.pos, a.W, w);
     bool ok = wk.refresh(sp, nullptr, nullptr);
     const double e_old = a.eloc[w];

@@ -1,0 +1,520 @@
+// sr_large.cu -- O_k of the neural Jastrow, the tensor-core S-matrix build
+// and the FP64 CG solve for stochastic reconfiguration with many parameters.
+#include <cuda_bf16.h>
+
+#include "sr_large.cuh"
+
+namespace mole {
+
+// --------------------------------------------------------------- O_k (network)
+
+constexpr int kNnMaxPairs = 8;
+
+struct OgenShared {
+  float W1[2][kNnH][kNnIn];
+  float b1[2][kNnH];
+  float W2[2][kNnH][kNnH];   // [a][c]
+  float W2T[2][kNnH][kNnH];  // [c][a]
+  float b2[2][kNnH];
+  float w3[2][kNnH];
+  float h1[kNnMaxPairs][kNnH];
+  float d2[kNnMaxPairs][kNnH];
+  double x[kMaxElec * 3];
+};
+
+// d J_nn / d theta for one walker per CTA iteration; thread a is hidden unit a.
+// J_nn = sum over pairs of y(pair), so each gradient is a sum over pairs;
+// dW2[a][c] = sum_p delta2[p][a] h1[p][c] is written with thread c writing
+// consecutive addresses.
+template <class T>
+__global__ void __launch_bounds__(kNnH) nn_ogen_kernel(const __grid_constant__ SysParams<float> sp, const double* pos,
+                                                       int W, int n_up, int N, T* O, int ldO, int col0) {
+  extern __shared__ __align__(16) unsigned char ogen_smem[];
+  OgenShared& sh = *reinterpret_cast<OgenShared*>(ogen_smem);
+  const int t = threadIdx.x;
+  for (int i = t; i < 2 * kNnNetP; i += kNnH) {
+    const int n = i / kNnNetP, k = i % kNnNetP;
+    const float v = (float)sp.nn_theta[i];
+    if (k < kNnOffB1) sh.W1[n][k / kNnIn][k % kNnIn] = v;
+    else if (k < kNnOffW2) sh.b1[n][k - kNnOffB1] = v;
+    else if (k < kNnOffB2) {
+      const int j = k - kNnOffW2;
+      sh.W2[n][j / kNnH][j % kNnH] = v;
+      sh.W2T[n][j % kNnH][j / kNnH] = v;
+    } else if (k < kNnOffW3) sh.b2[n][k - kNnOffB2] = v;
+    else if (k < kNnOffB3) sh.w3[n][k - kNnOffW3] = v;
+  }
+  __syncthreads();
+  for (int w = blockIdx.x; w < W; w += gridDim.x) {
+    if (t < 3 * N) sh.x[t] = pos[(size_t)t * W + w];
+    __syncthreads();
+    T* out = O + (size_t)w * ldO + col0;
+    for (int net = 0; net < 2; ++net) {
+      float gW1[kNnIn] = {0.f, 0.f, 0.f, 0.f}, gb1 = 0.f, gb2 = 0.f, gw3 = 0.f;
+      int np = 0;
+      const int n_b = net == 0 ? N : sp.n_nuc;
+      for (int i = 0; i < N; ++i)
+        for (int j = (net == 0 ? i + 1 : 0); j < n_b; ++j, ++np) {
+          double d0, d1, d2;
+          float s;
+          if (net == 0) {
+            d0 = sh.x[3 * i] - sh.x[3 * j];
+            d1 = sh.x[3 * i + 1] - sh.x[3 * j + 1];
+            d2 = sh.x[3 * i + 2] - sh.x[3 * j + 2];
+            s = ((i < n_up) == (j < n_up)) ? 1.f : 0.f;
+          } else {
+            d0 = sh.x[3 * i] - (double)sp.nuc_pos[3 * j];
+            d1 = sh.x[3 * i + 1] - (double)sp.nuc_pos[3 * j + 1];
+            d2 = sh.x[3 * i + 2] - (double)sp.nuc_pos[3 * j + 2];
+            s = sp.nuc_z[j];
+          }
+          const float r = (float)sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+          const float er = expf(-r);
+          const float x[kNnIn] = {r, er, s * r, s * er};
+          // layer 1 (thread a = unit a)
+          float z = sh.b1[net][t];
+#pragma unroll
+          for (int k = 0; k < kNnIn; ++k) z += sh.W1[net][t][k] * x[k];
+          const float h1 = tanhf(z);
+          sh.h1[np][t] = h1;
+          __syncthreads();
+          // layer 2 and output weight
+          float a2 = sh.b2[net][t];
+#pragma unroll 8
+          for (int c = 0; c < kNnH; ++c) a2 += sh.W2T[net][c][t] * sh.h1[np][c];
+          const float h2 = tanhf(a2);
+          const float dl2 = sh.w3[net][t] * (1.f - h2 * h2);
+          sh.d2[np][t] = dl2;
+          gb2 += dl2;
+          gw3 += h2;
+          __syncthreads();
+          // back to layer 1 (thread c = unit c)
+          float dl1 = 0.f;
+#pragma unroll 8
+          for (int a = 0; a < kNnH; ++a) dl1 += sh.W2[net][a][t] * sh.d2[np][a];
+          dl1 *= 1.f - h1 * h1;
+          gb1 += dl1;
+#pragma unroll
+          for (int k = 0; k < kNnIn; ++k) gW1[k] += dl1 * x[k];
+        }
+      T* o = out + net * kNnNetP;
+#pragma unroll
+      for (int k = 0; k < kNnIn; ++k) o[kNnOffW1 + t * kNnIn + k] = gW1[k];
+      o[kNnOffB1 + t] = gb1;
+      float hc[kNnMaxPairs];
+#pragma unroll
+      for (int p = 0; p < kNnMaxPairs; ++p) hc[p] = p < np ? sh.h1[p][t] : 0.f;
+      for (int a = 0; a < kNnH; ++a) {
+        float g = 0.f;
+#pragma unroll
+        for (int p = 0; p < kNnMaxPairs; ++p)
+          if (p < np) g += sh.d2[p][a] * hc[p];
+        o[kNnOffW2 + a * kNnH + t] = g;
+      }
+      o[kNnOffB2 + t] = gb2;
+      o[kNnOffW3 + t] = gw3;
+      if (t == 0) o[kNnOffB3] = (float)np;
+      __syncthreads();
+    }
+  }
+}
+
+template <class T>
+static cudaError_t launch_nn_ogen_t(const SysParams<float>& sp, const double* pos, int W, int n_up, int n_elec, T* O,
+                                   int ldO, int col0, int grid, cudaStream_t s) {
+  const size_t smem = sizeof(OgenShared);
+  cudaError_t e = cudaFuncSetAttribute(nn_ogen_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  nn_ogen_kernel<T><<<grid, kNnH, smem, s>>>(sp, pos, W, n_up, n_elec, O, ldO, col0);
+  return cudaGetLastError();
+}
+cudaError_t launch_nn_ogen(const SysParams<float>& sp, const double* pos, int W, int n_up, int n_elec, float* O,
+                           int ldO, int col0, int grid, cudaStream_t s) {
+  return launch_nn_ogen_t<float>(sp, pos, W, n_up, n_elec, O, ldO, col0, grid, s);
+}
+cudaError_t launch_nn_ogen64(const SysParams<float>& sp, const double* pos, int W, int n_up, int n_elec, double* O,
+                             int ldO, int col0, int grid, cudaStream_t s) {
+  return launch_nn_ogen_t<double>(sp, pos, W, n_up, n_elec, O, ldO, col0, grid, s);
+}
+
+__global__ void copy_cols_kernel(const double* src, int lds, int ncols, float* dst, int ldd, int W) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= W * ncols) return;
+  const int w = i / ncols, c = i % ncols;
+  dst[(size_t)w * ldd + c] = (float)src[(size_t)w * lds + c];
+}
+
+cudaError_t launch_copy_cols(const double* src, int lds, int ncols, float* dst, int ldd, int W, cudaStream_t s) {
+  if (ncols <= 0) return cudaSuccess;
+  copy_cols_kernel<<<(W * ncols + 255) / 256, 256, 0, s>>>(src, lds, ncols, dst, ldd, W);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------- centre + transpose
+
+// column sums of O[W][P] (FP64) into out[P]
+__global__ void column_sums_kernel(const float* O, int W, int P, int ldO, double* out, double scale) {
+  __shared__ double part[8][33];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int p = blockIdx.x * 32 + tx;
+  double s = 0.0;
+  if (p < P)
+    for (int w = ty; w < W; w += 8) s += (double)O[(size_t)w * ldO + p];
+  part[ty][tx] = s;
+  __syncthreads();
+  if (ty == 0 && p < P) {
+    double v = 0.0;
+    for (int k = 0; k < 8; ++k) v += part[k][tx];
+    out[p] = v * scale;
+  }
+}
+
+// Ot[p][w] = bf16(O[w][p] - c[p]); sumO[p] += sum_w (O - c), sumEO[p] += sum_w E (O - c)
+__global__ void center_transpose_kernel(const float* O, int W, int P, int ldO, const double* E, const double* c,
+                                        __nv_bfloat16* Ot, int K_pad, double* sumO, double* sumEO) {
+  __shared__ float tile[32][33];
+  __shared__ double e_s[32];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
+  const int p0 = blockIdx.x * 32, w0 = blockIdx.y * 32;
+  if (threadIdx.x < 32) e_s[threadIdx.x] = (w0 + threadIdx.x < W) ? E[w0 + threadIdx.x] : 0.0;
+  const int p = p0 + tx;
+  const double cp = p < P ? c[p] : 0.0;
+  double s1 = 0.0, s2 = 0.0;
+  __syncthreads();
+  for (int k = ty; k < 32; k += 8) {
+    const int w = w0 + k;
+    float v = 0.f;
+    if (p < P && w < W) {
+      const double d = (double)O[(size_t)w * ldO + p] - cp;
+      v = (float)d;
+      s1 += d;
+      s2 += e_s[k] * d;
+    }
+    tile[k][tx] = v;
+  }
+  __syncthreads();
+  for (int k = ty; k < 32; k += 8) {
+    const int pp = p0 + k, w = w0 + tx;
+    if (pp < P && w < W) Ot[(size_t)pp * K_pad + w] = __float2bfloat16_rn(tile[tx][k]);
+  }
+  if (p < P) {
+    atomicAdd(&sumO[p], s1);
+    atomicAdd(&sumEO[p], s2);
+  }
+}
+
+cudaError_t launch_center_transpose(const float* O, int W, int P, int ldO, const double* E, double* center,
+                                    bool set_center, __nv_bfloat16* Ot, int K_pad, double* sumO, double* sumEO,
+                                    double* scratch, cudaStream_t s) {
+  (void)scratch;
+  if (set_center) column_sums_kernel<<<(P + 31) / 32, 256, 0, s>>>(O, W, P, ldO, center, 1.0 / W);
+  dim3 grid((P + 31) / 32, (W + 31) / 32);
+  center_transpose_kernel<<<grid, 256, 0, s>>>(O, W, P, ldO, E, center, Ot, K_pad, sumO, sumEO);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------ S = Ot Ot^T on tcgen05
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: gives up after about a second of SM clock and reports false.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, phase))
+    if (clock64() - t0 > 2000000000LL) return false;
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1,024 bytes apart, descriptor version 1.
+__device__ __forceinline__ uint64_t umma_desc_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)(16u >> 4) << 16;
+  d |= (uint64_t)(1024u >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+// Instruction descriptor of kind::f16: BF16 A and B, FP32 accumulator,
+// both K-major, M = 128, N = 128.
+constexpr uint32_t kSIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kSBM >> 3) << 17) |
+                             ((uint32_t)(kSBM >> 4) << 24);
+
+__device__ __forceinline__ void umma_f16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__global__ void __launch_bounds__(128, 1) s_gemm_kernel(const __grid_constant__ CUtensorMap tmap, double* S, int P_pad,
+                                                        int K_pad, int* status) {
+  extern __shared__ __align__(1024) unsigned char gemm_smem[];
+  const uintptr_t base = ((uintptr_t)gemm_smem + 1023) & ~(uintptr_t)1023;
+  unsigned char* tiles = (unsigned char*)base;  // [stage][A | B]
+  uint64_t* full = (uint64_t*)(tiles + 2 * kSStages * kSTileBytes);
+  uint64_t* empty = full + kSStages;
+  uint64_t* done = empty + kSStages;
+  uint32_t* tmem_slot = (uint32_t*)(done + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  // upper-triangular tile (ti <= tj) of this CTA
+  const int T = P_pad / kSBM;
+  int ti = 0, rem = blockIdx.x;
+  while (rem >= T - ti) {
+    rem -= T - ti;
+    ++ti;
+  }
+  const int tj = ti + rem;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kSStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 2) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(128u));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = *tmem_slot;
+  const int nk = K_pad / kSBK;
+  bool ok = true;
+
+  if (warp == 0 && lane == 0) {
+    for (int kb = 0; kb < nk && ok; ++kb) {
+      const int s = kb % kSStages;
+      if (kb >= kSStages) ok = mbar_wait(&empty[s], ((kb / kSStages) - 1) & 1);
+      if (!ok) break;
+      mbar_expect_tx(&full[s], 2 * kSTileBytes);
+      tma_load_2d(tiles + (2 * s) * kSTileBytes, &tmap, kb * kSBK, ti * kSBM, &full[s]);
+      tma_load_2d(tiles + (2 * s + 1) * kSTileBytes, &tmap, kb * kSBK, tj * kSBM, &full[s]);
+    }
+  } else if (warp == 1 && lane == 0) {
+    for (int kb = 0; kb < nk && ok; ++kb) {
+      const int s = kb % kSStages;
+      ok = mbar_wait(&full[s], (kb / kSStages) & 1);
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t a0 = smem_u32(tiles + (2 * s) * kSTileBytes);
+      const uint32_t b0 = smem_u32(tiles + (2 * s + 1) * kSTileBytes);
+#pragma unroll
+      for (int kk = 0; kk < kSBK / 16; ++kk)
+        umma_f16(tmem, umma_desc_sw128(a0 + kk * 32), umma_desc_sw128(b0 + kk * 32), kSIdesc,
+                 (kb | kk) != 0 ? 1u : 0u);
+      umma_commit(&empty[s]);
+    }
+    umma_commit(done);
+  }
+  __syncwarp();
+  // epilogue: every thread owns one row of the 128 x 128 tile
+  const bool got = mbar_wait(done, 0);
+  if (!ok || !got) {
+    if (lane == 0) atomicOr(status, 4);
+  } else {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const int row = warp * 32 + lane;
+    double* out = S + (size_t)(ti * kSBM + row) * P_pad + tj * kSBM;
+#pragma unroll 1
+    for (int c0 = 0; c0 < kSBM; c0 += 16) {
+      uint32_t v[16];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+          "%14, %15}, [%16];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+            "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+      for (int i = 0; i < 16; ++i) out[c0 + i] += (double)__uint_as_float(v[i]);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 2) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(128u));
+}
+
+cudaError_t launch_s_gemm(const CUtensorMap* tmap, double* S, int P_pad, int K_pad, int* status, cudaStream_t s) {
+  const int T = P_pad / kSBM;
+  const int tiles = T * (T + 1) / 2;
+  cudaError_t e = cudaFuncSetAttribute(s_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSGemmSmem);
+  if (e != cudaSuccess) return e;
+  s_gemm_kernel<<<tiles, 128, kSGemmSmem, s>>>(*tmap, S, P_pad, K_pad, status);
+  return cudaGetLastError();
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+cudaError_t encode_ot_tensor_map(CUtensorMap* tmap, __nv_bfloat16* Ot, int P_pad, int K_pad) {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p) return cudaErrorNotSupported;
+    fn = (EncodeTiledFn)p;
+  }
+  const cuuint64_t dims[2] = {(cuuint64_t)K_pad, (cuuint64_t)P_pad};
+  const cuuint64_t strides[1] = {(cuuint64_t)K_pad * sizeof(__nv_bfloat16)};
+  const cuuint32_t box[2] = {(cuuint32_t)kSBK, (cuuint32_t)kSBM};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = fn(tmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)Ot, dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+// ------------------------------------------------------------ finalize S
+
+__global__ void finalize_s_kernel(double* S, int P, int P_pad, const double* sumO, double inv_n, double eps) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y;
+  if (j >= P || j < i) return;
+  const double mi = sumO[i] * inv_n, mj = sumO[j] * inv_n;
+  double v = S[(size_t)i * P_pad + j] * inv_n - mi * mj;
+  if (i == j) v += eps;
+  S[(size_t)i * P_pad + j] = v;
+  S[(size_t)j * P_pad + i] = v;
+}
+
+cudaError_t launch_finalize_s(double* S, int P, int P_pad, const double* sumO, double n, double eps, cudaStream_t s) {
+  dim3 grid((P + 255) / 256, P);
+  finalize_s_kernel<<<grid, 256, 0, s>>>(S, P, P_pad, sumO, 1.0 / n, eps);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------- CG
+
+// y = S x, one warp per row
+__global__ void gemv_rows_kernel(const double* S, int P, int ld, const double* x, double* y) {
+  const int row = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= P) return;
+  const double* r = S + (size_t)row * ld;
+  double s = 0.0;
+  for (int k = lane; k < P; k += 32) s += r[k] * x[k];
+  s = warp_sum(s);
+  if (lane == 0) y[row] = s;
+}
+
+// out = sum_i a_i b_i (one CTA, fixed order)
+__global__ void dot_kernel(const double* a, const double* b, int n, double* out) {
+  __shared__ double part[32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += a[i] * b[i];
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < blockDim.x / 32 ? part[threadIdx.x] : 0.0;
+    v = warp_sum(v);
+    if (threadIdx.x == 0) *out = v;
+  }
+}
+
+// scal[0] = r.z, scal[1] = p.q; alpha = r.z / p.q; x += alpha p; r -= alpha q; z = r / diag
+__global__ void cg_update_kernel(double* x, double* r, double* z, const double* p, const double* q, const double* dg,
+                                 const double* scal, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double alpha = scal[0] / scal[1];
+  x[i] += alpha * p[i];
+  r[i] -= alpha * q[i];
+  z[i] = r[i] / dg[i];
+}
+// p = z + beta p, beta = rz_new / rz_old (scal[2] / scal[0])
+__global__ void cg_direction_kernel(double* p, const double* z, double* scal, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  p[i] = z[i] + (scal[2] / scal[0]) * p[i];
+}
+__global__ void cg_shift_kernel(double* scal) { scal[0] = scal[2]; }
+__global__ void diag_kernel(const double* S, int P, int ld, double* dg, const double* b, double* r, double* z,
+                            double* p, double* x) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P) return;
+  dg[i] = S[(size_t)i * ld + i];
+  x[i] = 0.0;
+  r[i] = b[i];
+  z[i] = b[i] / dg[i];
+  p[i] = z[i];
+}
+
+cudaError_t sr_cg_solve(const double* S, int P, int ld, const double* b, double* x, double* work, int max_iter,
+                        double tol, int* iters, double* rel_res, cudaStream_t s) {
+  double* r = work;
+  double* z = r + P;
+  double* p = z + P;
+  double* q = p + P;
+  double* dg = q + P;
+  double* scal = dg + P;  // [0] rz, [1] pq, [2] rz_new, [3] rr, [4] bb
+  const int nb = (P + 255) / 256;
+  diag_kernel<<<nb, 256, 0, s>>>(S, P, ld, dg, b, r, z, p, x);
+  dot_kernel<<<1, 1024, 0, s>>>(r, z, P, scal);
+  dot_kernel<<<1, 1024, 0, s>>>(b, b, P, scal + 4);
+  double h[5];
+  int it = 0;
+  for (; it < max_iter; ++it) {
+    gemv_rows_kernel<<<(P + 7) / 8, 256, 0, s>>>(S, P, ld, p, q);
+    dot_kernel<<<1, 1024, 0, s>>>(p, q, P, scal + 1);
+    cg_update_kernel<<<nb, 256, 0, s>>>(x, r, z, p, q, dg, scal, P);
+    dot_kernel<<<1, 1024, 0, s>>>(r, z, P, scal + 2);
+    cg_direction_kernel<<<nb, 256, 0, s>>>(p, z, scal, P);
+    cg_shift_kernel<<<1, 1, 0, s>>>(scal);
+    if ((it + 1) % 10 == 0 || it + 1 == max_iter) {
+      dot_kernel<<<1, 1024, 0, s>>>(r, r, P, scal + 3);
+      cudaError_t e = cudaMemcpyAsync(h, scal, sizeof(h), cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) return e;
+      if (h[3] <= tol * tol * h[4]) {
+        ++it;
+        break;
+      }
+    }
+  }
+  cudaError_t e = cudaMemcpyAsync(h, scal, sizeof(h), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (iters) *iters = it;
+  if (rel_res) *rel_res = h[4] > 0 ? sqrt(h[3] / h[4]) : 0.0;
+  return e != cudaSuccess ? e : cudaGetLastError();
+}
+
+}  // namespace mole

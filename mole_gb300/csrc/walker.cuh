@@ -18,6 +18,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "nn.cuh"
 #include "normal.cuh"
 
 namespace mole {
@@ -45,6 +46,7 @@ struct SysParams {
   R half_omega2;
   double vnn;  // n-n repulsion constant
   int n_exp, P, off_ee, off_en, off_nn;
+  const double* nn_theta;  // device copy of the 9,090 network parameters (neural systems)
 };
 
 template <class R>
@@ -83,8 +85,18 @@ struct OneBody {
   R ven;
 };
 
-template <class R, int n, int NZ, bool EN>
-__device__ __forceinline__ void one_body(const SysParams<R>& sp, int spin, const R (&r)[3], OneBody<R, n, NZ>& o) {
+// Neural-Jastrow context of a thread: the CTA's shared weights and this
+// thread's hidden-layer jet scratch (element stride `stride`).
+template <class R>
+struct NnCtx {
+  const NnShared<R>* sh;
+  R* scr;
+  int stride;
+};
+
+template <class R, int n, int NZ, bool EN, bool NN = false>
+__device__ __forceinline__ void one_body(const SysParams<R>& sp, int spin, const R (&r)[3], OneBody<R, n, NZ>& o,
+                                         const NnCtx<R>* nn = nullptr) {
 #pragma unroll
   for (int k = 0; k < OneBody<R, n, NZ>::nm; ++k) {
     o.val[k] = 0;
@@ -168,6 +180,16 @@ __device__ __forceinline__ void one_body(const SysParams<R>& sp, int spin, const
       o.ljen += (R)-2 * A * sp.en_a * q * q * q + (R)2 * A * q * q * inv;
       if constexpr (NZ > 0) o.djen += -A * rr * rr * q * q;
     }
+    if constexpr (NN) {
+      R y, y1, y2;
+      nn_jet<R>(nn->sh->net[1], rr, sp.nuc_z[I], nn->scr, nn->stride, y, y1, y2);
+      const R f = y1 * inv;
+      o.jen += y;
+      o.gjen[0] += f * d0;
+      o.gjen[1] += f * d1;
+      o.gjen[2] += f * d2;
+      o.ljen += y2 + (R)2 * f;
+    }
   }
 }
 
@@ -178,9 +200,11 @@ struct PairVals {
   R rs;  // scaled distance R(r) of the Pade term
 };
 
-// Pade pair term (theory/jastrow.tex:15-126) at separation d = r_i - r_j.
-template <class R, int PM>
-__device__ __forceinline__ void pair_vals(const SysParams<R>& sp, bool same, R d0, R d1, R d2, PairVals<R, PM>& v) {
+// Pade pair term (theory/jastrow.tex:15-126) at separation d = r_i - r_j,
+// plus the e-e network when NN.
+template <class R, int PM, bool NN = false>
+__device__ __forceinline__ void pair_vals(const SysParams<R>& sp, bool same, R d0, R d1, R d2, PairVals<R, PM>& v,
+                                          const NnCtx<R>* nn = nullptr) {
   const R r2 = d0 * d0 + d1 * d1 + d2 * d2;
   const R inv = rsqrt_t<R>(r2);
   const R r = r2 * inv;
@@ -190,6 +214,13 @@ __device__ __forceinline__ void pair_vals(const SysParams<R>& sp, bool same, R d
   v.l = 0;
   v.db = 0;
   v.rs = r;
+  if constexpr (NN) {
+    R y, y1, y2;
+    nn_jet<R>(nn->sh->net[0], r, same ? (R)1 : (R)0, nn->scr, nn->stride, y, y1, y2);
+    v.u = y;
+    v.f = y1 * inv;
+    v.l = y2 + (R)2 * v.f;
+  }
   if (!sp.ee_on) return;
   const R cusp = same ? sp.cusp_para : sp.cusp_anti;
   R Rs = r, Rp = 1, Rpp = 0;
@@ -214,10 +245,11 @@ __device__ __forceinline__ void pair_vals(const SysParams<R>& sp, bool same, R d
     Rk *= Rs;
   }
   const R du = uR * Rp;
+  const R f = du * inv;
   v.rs = Rs;
-  v.u = val;
-  v.f = du * inv;
-  v.l = uRR * Rp * Rp + uR * Rpp + (R)2 * v.f;
+  v.u += val;
+  v.f += f;
+  v.l += uRR * Rp * Rp + uR * Rpp + (R)2 * f;
 }
 
 // In-register Gauss-Jordan inverse with partial pivoting; row swaps are
@@ -281,8 +313,9 @@ __device__ __forceinline__ bool gj_invert(double (&a)[n * n], double (&inv)[n * 
 // Walker state and moves for spin blocks of NU up and ND down electrons;
 // PM > 0 also caches what the first PM parameter derivatives need; EN
 // compiles the e-n Jastrow term in (its caches fold away when it is off).
-template <int NU, int ND, class R, int PM, bool EN>
+template <int NU, int ND, class R, int PM, bool EN, bool NN = false>
 struct Walker {
+  NnCtx<R> nn;  // shared-memory weights and jet scratch when NN
   static constexpr int N = NU + ND;
   static constexpr int NDm = ND > 0 ? ND : 1;
   static constexpr int NMAX = NU > NDm ? NU : NDm;
@@ -370,7 +403,7 @@ struct Walker {
       R r[3];
       rpos(e, r);
       OneBody<R, n, NZ> o;
-      one_body<R, n, NZ, EN>(sp, isup ? 0 : 1, r, o);
+      one_body<R, n, NZ, EN, NN>(sp, isup ? 0 : 1, r, o, &nn);
 #pragma unroll
       for (int k = 0; k < n; ++k) {
         if constexpr (isup) au[i * NU + k] = (double)o.val[k];
@@ -389,8 +422,8 @@ struct Walker {
       static_for<i + 1, N>([&](auto jc) {
         constexpr int j = decltype(jc)::value;
         PairVals<R, PM> v;
-        pair_vals<R, PM>(sp, same_spin(i, j), (R)(x[i][0] - x[j][0]), (R)(x[i][1] - x[j][1]),
-                         (R)(x[i][2] - x[j][2]), v);
+        pair_vals<R, PM, NN>(sp, same_spin(i, j), (R)(x[i][0] - x[j][0]), (R)(x[i][1] - x[j][1]),
+                             (R)(x[i][2] - x[j][2]), v, &nn);
         put_pair(pidx(i, j), v);
         J += (double)v.u;
       });
@@ -484,7 +517,7 @@ struct Walker {
     const double xn[3] = {x[e][0] + dx[0], x[e][1] + dx[1], x[e][2] + dx[2]};
     const R rn[3] = {(R)xn[0], (R)xn[1], (R)xn[2]};
     OneBody<R, n, NZ> o;
-    one_body<R, n, NZ, EN>(sp, isup ? 0 : 1, rn, o);
+    one_body<R, n, NZ, EN, NN>(sp, isup ? 0 : 1, rn, o, &nn);
     double ratio = 0.0;
 #pragma unroll
     for (int k = 0; k < n; ++k) ratio += (double)o.val[k] * B[k * ld + i];
@@ -495,7 +528,8 @@ struct Walker {
     static_for<0, N>([&](auto jc) {
       constexpr int j = decltype(jc)::value;
       if constexpr (j != e) {
-        pair_vals<R, PM>(sp, same_spin(e, j), rn[0] - (R)x[j][0], rn[1] - (R)x[j][1], rn[2] - (R)x[j][2], pv[j]);
+        pair_vals<R, PM, NN>(sp, same_spin(e, j), rn[0] - (R)x[j][0], rn[1] - (R)x[j][1], rn[2] - (R)x[j][2], pv[j],
+                             &nn);
         dJ += pv[j].u - pu[pidx(e, j)];
       }
     });

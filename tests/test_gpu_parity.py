@@ -34,7 +34,15 @@ def systems():
                   en_coef=[-0.3])
     return {"He": he, "H2": S.h2(), "He-kappa-poly": kap, "H2+": S.h2_ion_product(1.0, 2.5),
             "SHO": S.sho_gaussian(1.3, 0.9), "H-gauss": S.hydrogen_gaussian(1.0), "Be": S.beryllium(),
-            "LiH": S.lih(neural=False), "Li-2p": li, "Z-atom-4e": S.random_atom(rng, n_range=(4, 4))}
+            "LiH": S.lih(neural=False), "Li-2p": li, "Z-atom-4e": S.random_atom(rng, n_range=(4, 4)),
+            "LiH-nn": S.lih(neural=True, rng=np.random.default_rng(21)),
+            "Be-nn": _scaled_nn(S.beryllium(neural=True, rng=np.random.default_rng(22)), 0.2)}
+
+
+def _scaled_nn(s, std):
+    """Network weights of a given spread, so the networks' terms are not negligible."""
+    w = np.random.default_rng(5).normal(0.0, std, size=s.nn_weights.size)
+    return s.with_params(np.concatenate([s.params()[:-w.size], w]))
 
 
 @pytest.mark.parametrize("name", list(systems().keys()))
@@ -57,7 +65,7 @@ def test_eval_matches_oracle_fp64(ctx, name):
     np.testing.assert_array_equal(wk.positions(), pos)
 
 
-@pytest.mark.parametrize("name", ["He", "H2", "Be", "LiH", "Li-2p"])
+@pytest.mark.parametrize("name", ["He", "H2", "Be", "LiH", "Li-2p", "LiH-nn", "Be-nn"])
 def test_eval_mixed_precision_close(ctx, name):
     s = systems()[name]
     wf = api.WaveFunction(ctx, s)
@@ -65,7 +73,7 @@ def test_eval_mixed_precision_close(ctx, name):
     pos = np.random.default_rng(9).normal(size=(W, s.n_elec, 3)) * 1.3
     wk = api.Walkers(wf, W)
     wk.set_positions(pos)
-    g = wk.evaluate(api.PREC_MIXED)
+    g = wk.evaluate(api.PREC_MIXED, want_O=s.n_params <= 8)
     r = O.evaluate(s, pos)
     # FP32 orbitals/Jastrow with FP64 contraction and assembly
     assert close(g["eloc"], r["eloc"], floor=1.0) < 2e-4
@@ -73,7 +81,8 @@ def test_eval_mixed_precision_close(ctx, name):
 
 
 @pytest.mark.parametrize("name,move,step", [("He", 0, 0.5), ("H2", 1, 0.4), ("He", 2, 0.1), ("Be", 1, 0.3),
-                                            ("Be", 2, 0.05), ("LiH", 0, 0.6), ("H2+", 0, 1.0), ("Li-2p", 2, 0.08)])
+                                            ("Be", 2, 0.05), ("LiH", 0, 0.6), ("H2+", 0, 1.0), ("Li-2p", 2, 0.08),
+                                            ("LiH-nn", 1, 0.3), ("Be-nn", 2, 0.05)])
 def test_vmc_trajectory_matches_oracle(ctx, name, move, step):
     s = systems()[name]
     wf = api.WaveFunction(ctx, s)
