@@ -109,6 +109,69 @@ def cpu_baseline_sample(threads: int, walkers: int, sweeps: int):
     return walkers * sweeps / secs, secs, e
 
 
+def lih_time_to_sigma(ctx, W: int, train_iters: int, target: float = 1e-3) -> dict:
+    """LiH (configs[3] geometry): the plain form (Slater x Pade, FP64, SR over
+    the orbital exponents and b) against the neural form (network Jastrow,
+    FP32 evaluation / FP64 accumulation, SR over all 9,094 parameters on the
+    tensor cores), both trained from the same start; then each samples until
+    the blocking error of E reaches `target` Ha. Reports the sampling wall
+    time, energies, variances, throughput and the SR-GEMM roofline."""
+    import numpy as np
+    import torch
+
+    from mole_gb300 import api, flop_model
+    from mole_gb300 import system as S
+
+    out = {}
+    for name, neural, prec in (("plain_fp64", False, api.PREC_FP64), ("neural_mixed", True, api.PREC_MIXED)):
+        s = S.lih(neural=neural, rng=np.random.default_rng(1))
+        wf = api.WaveFunction(ctx, s)
+        wk = api.Walkers(wf, W, seed=0x5EED + 4)
+        samp = api.Sampler(wf, api.MetropolisGaussian(0.3), wk, precision=prec)
+        samp.run(300, 0, 1)
+        sr = api.StochasticReconfiguration(0.05, 1e-3, samples=4, sample_every=10, precision=prec)
+        ctx.enable_timing(True)
+        t0 = time.perf_counter()
+        api.VmcRunner(samp, sr).run_optimization(train_iters, 120, 20)
+        torch.cuda.synchronize()
+        train_s = time.perf_counter() - t0
+        g_ms, g_n = ctx.kernel_time(3)
+        v_ms, v_n = ctx.kernel_time(0)
+        ctx.enable_timing(False)
+        samp.run(100, 0, 1)
+        torch.cuda.synchronize()
+        mom = np.zeros(7)
+        sweeps = 0
+        t0 = time.perf_counter()
+        while True:
+            r = samp.run(0, 20, 10)
+            mom += r.moments
+            sweeps += 20
+            err = api.blocking_error(mom)
+            if err <= target or sweeps >= 20000:
+                break
+        torch.cuda.synchronize()
+        secs = time.perf_counter() - t0
+        E = mom[1] / mom[0]
+        leg = {"time_to_sigma_s": secs, "sweeps": sweeps, "energy": E, "error": err,
+               "variance": mom[2] / mom[0] - E * E, "walker_steps_per_s": W * sweeps / secs,
+               "train_s": train_s, "train_iters": train_iters, "vmc_kernel_ms_per_launch": v_ms / max(v_n, 1)}
+        if neural and g_n:
+            P_pad = (s.n_params + 127) // 128 * 128
+            flops = 2.0 * P_pad * P_pad * ((W + 63) // 64 * 64) * 0.5 * (1 + 128.0 / P_pad)  # upper tiles only
+            leg["s_gemm"] = {"ms_per_launch": g_ms / g_n, "tflops": flops / (g_ms / g_n * 1e-3) / 1e12,
+                             "peak_bf16_tflops": 1935.3, "peak_source": "MEASURED_PEAKS.json bf16 burst"}
+        out[name] = leg
+        wk.close()
+        wf.close()
+    out["neural_faster"] = out["neural_mixed"]["time_to_sigma_s"] < out["plain_fp64"]["time_to_sigma_s"]
+    out["neural_energy_not_higher"] = out["neural_mixed"]["energy"] <= out["plain_fp64"]["energy"] + 2 * np.hypot(
+        out["neural_mixed"]["error"], out["plain_fp64"]["error"])
+    out["target_ha"] = target
+    out["walkers"] = W
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_info()
     if rank != 0:
@@ -276,6 +339,9 @@ def main():
                              "energy": res2[-1].energy, "energy_error": res2[-1].error,
                              "energy_fp64_same_params": r_fp64.energy, "energy_fp64_error": r_fp64.error,
                              "energy_delta_vs_fp64": res2[-1].energy - r_fp64.energy}
+        # -------------------------------------------------- neural vs plain, LiH
+        if rank == 0 and world == 1:
+            line["lih_time_to_sigma"] = lih_time_to_sigma(ctx, 16384, 20)
         # -------------------------------------------------- CPU baseline
         if rank == 0 and world == 1:
             from oracle import oracle as O

@@ -145,8 +145,9 @@ int mole_ctx_set_stream(mole_ctx* ctx, void* cuda_stream);
 int mole_sync(mole_ctx* ctx);
 /* Per-kernel CUDA-event timing of the hot kernels (off by default). */
 int mole_ctx_enable_timing(mole_ctx* ctx, int32_t on);
-/* kernel: 0 = VMC sweep kernel, 1 = DMC step kernel, 2 = eval kernel. Returns
- * the summed milliseconds and launch count since timing was enabled. */
+/* kernel: 0 = VMC sweep kernel, 1 = DMC step sequence, 2 = evaluation (and
+ * O_k generation), 3 = tensor-core S-matrix GEMM. Returns the summed
+ * milliseconds and launch count since timing was enabled. */
 int mole_ctx_kernel_time(mole_ctx* ctx, int32_t kernel, double* total_ms, int64_t* launches);
 /* Device FP64 and FP32 FMA peaks measured by a microbenchmark (GFLOP/s). */
 int mole_probe_peaks(mole_ctx* ctx, double* fp64_gflops, double* fp32_gflops);

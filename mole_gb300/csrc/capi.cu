@@ -79,8 +79,8 @@ struct mole_ctx {
   cudaStream_t own = nullptr;
   cudaStream_t stream = nullptr;
   bool timing = false;
-  double kernel_ms[3] = {0, 0, 0};
-  int64_t kernel_launches[3] = {0, 0, 0};
+  double kernel_ms[4] = {0, 0, 0, 0};  // VMC sweep, DMC step, evaluation, S-matrix GEMM
+  int64_t kernel_launches[4] = {0, 0, 0, 0};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   DevBuf<double> partials, tb_partials, reduced, scratch;
   DevBuf<int> status;
@@ -328,7 +328,7 @@ int mole_sync(mole_ctx* c) {
 int mole_ctx_enable_timing(mole_ctx* c, int32_t on) {
   if (!c) return fail(MOLE_ERR_INVALID_ARG, "ctx is NULL");
   c->timing = on != 0;
-  for (int k = 0; k < 3; ++k) {
+  for (int k = 0; k < 4; ++k) {
     c->kernel_ms[k] = 0;
     c->kernel_launches[k] = 0;
   }
@@ -336,7 +336,7 @@ int mole_ctx_enable_timing(mole_ctx* c, int32_t on) {
 }
 
 int mole_ctx_kernel_time(mole_ctx* c, int32_t kernel, double* total_ms, int64_t* launches) {
-  if (!c || kernel < 0 || kernel > 2) return fail(MOLE_ERR_INVALID_ARG, "bad ctx or kernel id");
+  if (!c || kernel < 0 || kernel > 3) return fail(MOLE_ERR_INVALID_ARG, "bad ctx or kernel id");
   if (total_ms) *total_ms = c->kernel_ms[kernel];
   if (launches) *launches = c->kernel_launches[kernel];
   return MOLE_OK;
@@ -927,9 +927,11 @@ int mole_sr_collect_sample(mole_walkers* w, int32_t precision) {
                             c->stream));
   CUDA_TRY(launch_center_transpose(t->O, W, P, P, t->E, t->center, !t->have_center, t->Ot, t->K_pad, t->sumO,
                                    t->sumEO, nullptr, c->stream));
-  t->have_center = true;
-  CUDA_TRY(launch_s_gemm(w->srl_map, t->S, t->P_pad, t->K_pad, t->status, c->stream));
   tm.stop();
+  t->have_center = true;
+  Timer tg(c, 3);
+  CUDA_TRY(launch_s_gemm(w->srl_map, t->S, t->P_pad, t->K_pad, t->status, c->stream));
+  tg.stop();
   std::vector<double> e(W);
   CUDA_TRY(cudaMemcpyAsync(e.data(), t->E, sizeof(double) * W, cudaMemcpyDeviceToHost, c->stream));
   int st = 0;
