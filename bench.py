@@ -45,7 +45,49 @@ def parse():
     p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     p.add_argument("--no-extras", action="store_true", help="skip the e2e, mixed and CPU-baseline legs")
     p.add_argument("--no-clocks", action="store_true", help="do not sample nvidia-smi during the timed region")
+    p.add_argument("--case", default=None, choices=["h2-vmc", "lih-nn-vmc", "sgemm", "be-dmc"],
+                   help="run one small kernel case (for profiling) and exit")
     return p.parse_args()
+
+
+def run_case(case: str) -> None:
+    """Small single-purpose runs whose kernels the committed ncu summaries profile."""
+    import numpy as np
+    import torch
+
+    from mole_gb300 import api
+    from mole_gb300 import system as S
+
+    ctx = api.Context(0)
+    t0 = time.perf_counter()
+    if case == "h2-vmc":
+        wf = api.WaveFunction(ctx, S.h2(1.0, 0.5))
+        wk = api.Walkers(wf, 65536)
+        samp = api.Sampler(wf, api.MetropolisGaussian(0.4), wk)
+        samp.run(20, 0, 1)
+        r = samp.run(0, 50, 10, sr=True)
+    elif case in ("lih-nn-vmc", "sgemm"):
+        wf = api.WaveFunction(ctx, S.lih(neural=True, rng=np.random.default_rng(1)))
+        wk = api.Walkers(wf, 16384)
+        samp = api.Sampler(wf, api.MetropolisGaussian(0.3), wk, precision=api.PREC_MIXED)
+        samp.run(20, 0, 1)
+        if case == "lih-nn-vmc":
+            r = samp.run(0, 20, 10)
+        else:
+            wk.sr_collect_begin()
+            for _ in range(2):
+                wk.sr_collect_sample(api.PREC_MIXED)
+            wk.sr_collect_solve(1e-3, 0.05)
+            r = None
+    else:  # be-dmc
+        wf = api.WaveFunction(ctx, S.beryllium())
+        wk = api.Walkers(wf, 131072)
+        api.Sampler(wf, api.MetropolisDiffuse(0.005), wk).run(20, 0, 1)
+        dmc = api.DmcRunner(wf, wk, -14.6)
+        r = dmc.run_block(0.005, 20)
+    torch.cuda.synchronize()
+    print(json.dumps({"case": case, "seconds": time.perf_counter() - t0,
+                      "energy": None if r is None else float(np.mean(r.energy if hasattr(r, "energy") else r))}))
 
 
 def dist_info():
@@ -202,6 +244,8 @@ def run_reference(args):
 
 def main():
     args = parse()
+    if args.case:
+        return run_case(args.case)
     if args.impl == "reference":
         return run_reference(args)
 
