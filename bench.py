@@ -90,6 +90,11 @@ def run_case(case: str) -> None:
                       "energy": None if r is None else float(np.mean(r.energy if hasattr(r, "energy") else r))}))
 
 
+def _json_default(o):
+    """numpy scalars in the JSON line"""
+    return o.item() if hasattr(o, "item") else str(o)
+
+
 def dist_info():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -396,7 +401,7 @@ def main():
                                     "sample": f"{512 * threads} walkers x 2000 sweeps ({secs:.1f} s), reference call "
                                               "pattern (oracle/faithful.cpp), std::thread over all host cores"}
     if rank == 0:
-        print(json.dumps(line), flush=True)
+        print(json.dumps(line, default=_json_default), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
 
