@@ -146,9 +146,12 @@ int mole_sync(mole_ctx* ctx);
 /* Per-kernel CUDA-event timing of the hot kernels (off by default). */
 int mole_ctx_enable_timing(mole_ctx* ctx, int32_t on);
 /* kernel: 0 = VMC sweep kernel, 1 = DMC step sequence, 2 = evaluation (and
- * O_k generation), 3 = tensor-core S-matrix GEMM. Returns the summed
+ * O_k generation), 3 = tensor-core S-matrix GEMM, 4 = one batched VMC run
+ * (the replayed graph). Returns the summed
  * milliseconds and launch count since timing was enabled. */
 int mole_ctx_kernel_time(mole_ctx* ctx, int32_t kernel, double* total_ms, int64_t* launches);
+/* SM count and compute capability of the context's device (the key of tuned tiles). */
+int mole_ctx_device_info(mole_ctx* ctx, int32_t* n_sm, int32_t* cc_major, int32_t* cc_minor);
 /* Device FP64 and FP32 FMA peaks measured by a microbenchmark (GFLOP/s). */
 int mole_probe_peaks(mole_ctx* ctx, double* fp64_gflops, double* fp32_gflops);
 
@@ -252,6 +255,52 @@ int mole_sr_collect_solve(mole_walkers* w, double eps, double step, int32_t max_
                           double* grad, double* info);
 /* The finalised S matrix (P x P, row-major) of the collected samples. */
 int mole_sr_collect_matrix(mole_walkers* w, double eps, double* S);
+
+/* ------------------------------------------------------ batches of systems */
+/* A ragged batch of independent systems -- different electron counts (up to
+ * 5 + 5), parameters and walker counts -- advanced together by ONE persistent
+ * launch whose CTAs pull (system, walker group) work items from a device
+ * queue, most expensive first. It replaces running Runner::run /
+ * VmcRunner::run_optimization once per (system, chain)
+ * (src/montecarlo/src/montecarlo.rs:24-46, src/vmc/src/vmc.rs:43-106).
+ * Systems keep their handles (a batch holds a reference to each and re-reads
+ * parameters changed with mole_params_set before the next run). seeds[k] is
+ * system k's random-stream key: the batch follows exactly the streams of a
+ * mole_walkers set created with that seed and the same walker count. widths
+ * (may be NULL = all 1) are the per-system proposal widths, multiplied by
+ * opts->step at run time. Positions start N(0, 1) as in mole_walkers_create. */
+typedef struct mole_batch mole_batch;
+int mole_batch_create(mole_ctx* ctx, int32_t n_systems, mole_system* const* systems, const int32_t* n_walkers,
+                      const uint64_t* seeds, const double* widths, mole_batch** out);
+int mole_batch_destroy(mole_batch* b);
+int mole_batch_info(const mole_batch* b, int32_t* n_systems, int64_t* n_walkers);
+/* Philox-seeded start of every system (as mole_walkers_init) */
+int mole_batch_init(mole_batch* b, int32_t kind, double width);
+/* host float64 [W][N][3] of one system */
+int mole_batch_set_positions(mole_batch* b, int32_t system, const double* pos, int64_t n_values);
+int mole_batch_get_positions(mole_batch* b, int32_t system, double* pos, int64_t n_values);
+/* shared sweep counter of the batch (the random-stream position) */
+int mole_batch_get_step(const mole_batch* b, uint64_t* step);
+int mole_batch_set_step(mole_batch* b, uint64_t step);
+/* The sweep loop of Runner::run + Sampler::move_state/sample for every system
+ * at once (box or Gaussian single-electron moves with Sherman-Morrison
+ * updates, FP64 inverse refresh every opts->refresh sweeps, E_L every sampled
+ * sweep). moments[n_systems][MOLE_NMOM] as for mole_vmc_run. A run is a
+ * CUDA graph (counter resets, the persistent kernel, the per-system reduction
+ * and the result copy) captured on the first call with given options and
+ * replayed by later ones. opts->sr must be 0. */
+int mole_batch_vmc_run(mole_batch* b, const mole_vmc_opts* opts, double* moments);
+/* Tile autotuner: times the persistent kernel for every walkers-per-CTA tile
+ * in {32, 64, 96, 128, 192, 256} that fits an SM (grid = SMs x resident CTAs)
+ * on a copy of the positions (chains and streams are left untouched), keeps
+ * the fastest and reports up to n_candidates (tile, ms) pairs. */
+int mole_batch_autotune(mole_batch* b, const mole_vmc_opts* opts, int32_t n_candidates, int32_t* cand_wpb,
+                        double* cand_ms, int32_t* n_timed);
+int mole_batch_set_tile(mole_batch* b, int32_t walkers_per_cta);
+/* the tile in use and the persistent grid it launches for `precision` */
+int mole_batch_get_tile(const mole_batch* b, int32_t* walkers_per_cta, int32_t* ctas, int32_t precision);
+/* number of graph replays run so far */
+int mole_batch_graph_launches(const mole_batch* b, int64_t* n);
 
 /* ---------------------------------------------------------------------- DMC */
 /* DmcRunner::diffuse inner loop (src/dmc/src/dmc.rs:81-141) for opts->n_steps

@@ -69,6 +69,7 @@ SIGNATURES = {
     "mole_ctx_enable_timing": (C.c_int, [_P, C.c_int32]),
     "mole_ctx_kernel_time": (C.c_int, [_P, C.c_int32, _D, C.POINTER(C.c_int64)]),
     "mole_probe_peaks": (C.c_int, [_P, _D, _D]),
+    "mole_ctx_device_info": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "mole_system_create": (C.c_int, [_P, C.POINTER(SystemDesc), _D, C.c_int32, C.POINTER(_P)]),
     "mole_system_destroy": (C.c_int, [_P]),
     "mole_num_params": (C.c_int, [_P, C.POINTER(C.c_int32)]),
@@ -93,6 +94,21 @@ SIGNATURES = {
     "mole_sr_collect_solve": (C.c_int, [_P, C.c_double, C.c_double, C.c_int32, C.c_double, _D, _D, _D]),
     "mole_sr_collect_matrix": (C.c_int, [_P, C.c_double, _D]),
     "mole_dmc_run": (C.c_int, [_P, C.POINTER(DmcOpts), _D, _D]),
+    "mole_batch_create": (C.c_int, [_P, C.c_int32, C.POINTER(_P), C.POINTER(C.c_int32), C.POINTER(C.c_uint64), _D,
+                                    C.POINTER(_P)]),
+    "mole_batch_destroy": (C.c_int, [_P]),
+    "mole_batch_info": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int64)]),
+    "mole_batch_init": (C.c_int, [_P, C.c_int32, C.c_double]),
+    "mole_batch_set_positions": (C.c_int, [_P, C.c_int32, _D, C.c_int64]),
+    "mole_batch_get_positions": (C.c_int, [_P, C.c_int32, _D, C.c_int64]),
+    "mole_batch_get_step": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
+    "mole_batch_set_step": (C.c_int, [_P, C.c_uint64]),
+    "mole_batch_vmc_run": (C.c_int, [_P, C.POINTER(VmcOpts), _D]),
+    "mole_batch_autotune": (C.c_int, [_P, C.POINTER(VmcOpts), C.c_int32, C.POINTER(C.c_int32), _D,
+                                      C.POINTER(C.c_int32)]),
+    "mole_batch_set_tile": (C.c_int, [_P, C.c_int32]),
+    "mole_batch_get_tile": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int32]),
+    "mole_batch_graph_launches": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "mole_checkpoint_save": (C.c_int, [_P, C.c_char_p]),
     "mole_checkpoint_load": (C.c_int, [_P, C.c_char_p]),
 }

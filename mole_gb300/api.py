@@ -542,3 +542,182 @@ class DmcRunner:
     @property
     def acceptance(self) -> float:
         return self.accepted / max(self.proposed, 1.0)
+
+
+# ------------------------------------------------------------------ batches
+
+def _tile_cache_path() -> str:
+    import os
+
+    return os.environ.get("MOLE_GB300_TILE_CACHE",
+                          os.path.join(os.path.expanduser("~"), ".cache", "mole_gb300", "batch_tiles.json"))
+
+
+class Batch:
+    """A ragged batch of independent systems (each with its own walker
+    ensemble, electron count up to 5 + 5 and parameters) advanced by one
+    persistent launch replayed as a CUDA graph. It stands where the reference
+    runs Runner::run once per system and chain (src/montecarlo/src/montecarlo.rs:24-46,
+    src/vmc/src/vmc.rs:63-76).
+
+    ``systems`` are System descriptors or WaveFunctions; ``seeds[k]`` keys
+    system k's random streams exactly as ``Walkers(wf, W, seed)`` does;
+    ``widths[k]`` is system k's proposal width, multiplied by the move's step
+    at run time."""
+
+    def __init__(self, ctx: Context, systems, n_walkers, seeds=None, widths=None):
+        self.ctx, self.lib = ctx, ctx.lib
+        self.wfs = [s if isinstance(s, WaveFunction) else WaveFunction(ctx, s) for s in systems]
+        S = len(self.wfs)
+        self.n_walkers = np.ascontiguousarray(n_walkers, dtype=np.int32).reshape(S)
+        sd = np.arange(S, dtype=np.uint64) + np.uint64(0x5EED) if seeds is None else seeds
+        self.seeds = np.ascontiguousarray(sd, dtype=np.uint64).reshape(S)
+        self.widths = None if widths is None else np.ascontiguousarray(widths, dtype=np.float64).reshape(S)
+        hs = (C.c_void_p * S)(*[wf.h.value for wf in self.wfs])
+        h = C.c_void_p()
+        check(self.lib.mole_batch_create(ctx.h, S, hs, self.n_walkers.ctypes.data_as(C.POINTER(C.c_int32)),
+                                         self.seeds.ctypes.data_as(C.POINTER(C.c_uint64)), dptr(self.widths),
+                                         C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.mole_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __len__(self) -> int:
+        return len(self.wfs)
+
+    @property
+    def total_walkers(self) -> int:
+        return int(self.n_walkers.sum())
+
+    def electrons(self, k: int) -> int:
+        return self.wfs[k].num_electrons()
+
+    def init(self, kind: int = INIT_NORMAL, width: float = 1.0):
+        check(self.lib.mole_batch_init(self.h, kind, width))
+
+    def positions(self, k: int) -> np.ndarray:
+        p = np.zeros((int(self.n_walkers[k]), self.electrons(k), 3))
+        check(self.lib.mole_batch_get_positions(self.h, k, dptr(p), p.size))
+        return p
+
+    def set_positions(self, k: int, pos) -> None:
+        p = np.ascontiguousarray(pos, dtype=np.float64).reshape(int(self.n_walkers[k]), self.electrons(k), 3)
+        check(self.lib.mole_batch_set_positions(self.h, k, dptr(p), p.size))
+
+    @property
+    def step(self) -> int:
+        s = C.c_uint64()
+        check(self.lib.mole_batch_get_step(self.h, C.byref(s)))
+        return s.value
+
+    @step.setter
+    def step(self, v: int):
+        check(self.lib.mole_batch_set_step(self.h, int(v)))
+
+    def _opts(self, metropolis, n_eq, n_steps, block_size, precision, refresh):
+        return _lib.VmcOpts(metropolis.kind, metropolis.step, n_eq, n_steps, block_size, 0, precision, refresh)
+
+    def run(self, metropolis, n_eq: int, n_steps: int, block_size: int, precision: int = PREC_MIXED,
+            refresh: int = 100) -> list[MonteCarloResult]:
+        """One graph replay: n_eq + n_steps sweeps of every system; a
+        MonteCarloResult per system."""
+        o = self._opts(metropolis, n_eq, n_steps, block_size, precision, refresh)
+        mom = np.zeros((len(self), _lib.NMOM))
+        check(self.lib.mole_batch_vmc_run(self.h, C.byref(o), dptr(mom)))
+        out = []
+        for m in mom:
+            n = m[0]
+            E = m[1] / n if n else float("nan")
+            var = m[2] / n - E * E if n else float("nan")
+            out.append(MonteCarloResult(E, blocking_error(m), var, m[5] / max(m[6], 1.0), m, np.zeros(0)))
+        return out
+
+    @property
+    def tile(self) -> int:
+        w, c = C.c_int32(), C.c_int32()
+        check(self.lib.mole_batch_get_tile(self.h, C.byref(w), C.byref(c), PREC_MIXED))
+        return w.value
+
+    @tile.setter
+    def tile(self, walkers_per_cta: int):
+        check(self.lib.mole_batch_set_tile(self.h, int(walkers_per_cta)))
+
+    def grid(self, precision: int = PREC_MIXED) -> int:
+        w, c = C.c_int32(), C.c_int32()
+        check(self.lib.mole_batch_get_tile(self.h, C.byref(w), C.byref(c), precision))
+        return c.value
+
+    @property
+    def graph_launches(self) -> int:
+        n = C.c_int64()
+        check(self.lib.mole_batch_graph_launches(self.h, C.byref(n)))
+        return n.value
+
+    def tile_key(self, metropolis, precision: int) -> str:
+        """Cache key of a tuned tile: device (SMs, compute capability),
+        precision, move and the batch's largest spin blocks, electron-count
+        profile and total walkers (to a power of two)."""
+        n_sm, ma, mi = C.c_int32(), C.c_int32(), C.c_int32()
+        check(self.lib.mole_ctx_device_info(self.ctx.h, C.byref(n_sm), C.byref(ma), C.byref(mi)))
+        ns = sorted({self.electrons(k) for k in range(len(self))})
+        tot = 1 << max(int(self.total_walkers) - 1, 0).bit_length()
+        return f"sm{ma.value}{mi.value}x{n_sm.value}|p{precision}|m{metropolis.kind}|N{','.join(map(str, ns))}|W{tot}"
+
+    def autotune(self, metropolis, precision: int = PREC_MIXED, sweeps: int = 10, cache: bool = True) -> dict:
+        """Picks the walkers-per-CTA tile by timing every candidate on a copy of
+        the positions (the chains are untouched); with ``cache`` a tile tuned
+        before for the same key is reused from the JSON tile cache."""
+        import json
+        import os
+
+        key = self.tile_key(metropolis, precision)
+        path = _tile_cache_path()
+        table = {}
+        if cache and os.path.exists(path):
+            try:
+                with open(path) as f:
+                    table = json.load(f)
+            except (OSError, ValueError):
+                table = {}
+            if key in table:
+                self.tile = int(table[key]["tile"])
+                return {"tile": self.tile, "cached": True, "key": key, "timings": table[key].get("timings", {})}
+        o = self._opts(metropolis, 0, sweeps, sweeps, precision, 100)
+        wpb, ms, n = (C.c_int32 * 8)(), (C.c_double * 8)(), C.c_int32()
+        check(self.lib.mole_batch_autotune(self.h, C.byref(o), 8, wpb, ms, C.byref(n)))
+        timings = {int(wpb[i]): float(ms[i]) for i in range(n.value)}
+        res = {"tile": self.tile, "cached": False, "key": key, "timings": timings}
+        if cache:
+            table[key] = {"tile": res["tile"], "timings": {str(k): v for k, v in timings.items()}}
+            try:
+                os.makedirs(os.path.dirname(path), exist_ok=True)
+                with open(path + ".tmp", "w") as f:
+                    json.dump(table, f, indent=1, sort_keys=True)
+                os.replace(path + ".tmp", path)
+            except OSError:
+                pass
+        return res
+
+
+def ragged_batch(n_systems: int = 256, rng: np.random.Generator | None = None, w_range=(256, 4096),
+                 z_range=(2, 10), n_range=(2, 10)):
+    """The ragged-batch workload: n_systems atoms/ions from ``random_atom``
+    (Z in U{2..10}, N in U{2..10}, 1s/2s/2p STOs with exponents U[0.5, Z],
+    Pade e-e and e-n Jastrows), walker counts U{256..4096}, a Gaussian
+    proposal width 0.6 / sqrt(Z) each. Returns (systems, walkers, widths)."""
+    from .system import random_atom
+
+    rng = rng or np.random.default_rng(0x5EED + 2)
+    systems = [random_atom(rng, z_range=z_range, n_range=n_range) for _ in range(n_systems)]
+    walkers = rng.integers(w_range[0], w_range[1] + 1, size=n_systems)
+    widths = np.array([0.6 / math.sqrt(float(s.nuc_z[0])) for s in systems])
+    return systems, walkers, widths

@@ -8,9 +8,7 @@
 #include <vector>
 
 #include "../../include/mole_gpu.h"
-#include "dispatch.cuh"
-#include "ensemble.cuh"
-#include "sr_large.cuh"
+#include "handles.cuh"
 
 namespace mole {
 #define MOLE_DECL(NU, ND)                           \
@@ -44,6 +42,11 @@ int fail(int code, const std::string& msg) {
   g_err = msg;
   return code;
 }
+}  // namespace
+
+int mole::set_error(int code, const std::string& msg) { return fail(code, msg); }
+
+namespace {
 
 #define CUDA_TRY(x)                                                                        \
   do {                                                                                     \
@@ -51,81 +54,7 @@ int fail(int code, const std::string& msg) {
     if (e_ != cudaSuccess) return fail(MOLE_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
-// Device buffer grown on demand (the context owns device memory).
-template <class T>
-struct DevBuf {
-  T* p = nullptr;
-  size_t n = 0;
-  cudaError_t reserve(size_t m) {
-    if (m <= n) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
-    cudaError_t e = cudaMalloc(&p, std::max<size_t>(m, 1) * sizeof(T));
-    if (e == cudaSuccess) n = m;
-    return e;
-  }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
-  }
-};
 }  // namespace
-
-struct mole_ctx {
-  int device = 0;
-  int n_sm = 0;
-  cudaStream_t own = nullptr;
-  cudaStream_t stream = nullptr;
-  bool timing = false;
-  double kernel_ms[4] = {0, 0, 0, 0};  // VMC sweep, DMC step, evaluation, S-matrix GEMM
-  int64_t kernel_launches[4] = {0, 0, 0, 0};
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  DevBuf<double> partials, tb_partials, reduced, scratch;
-  DevBuf<int> status;
-  int refs = 1;
-  bool closed = false;
-};
-
-struct mole_system {
-  mole_ctx* ctx = nullptr;
-  int n_nuc = 0, n_up = 0, n_dn = 0, n_basis = 0, n_exp = 0;
-  std::vector<double> nuc_pos, en_coef, coef_up, coef_dn;
-  std::vector<int> nuc_z, b_center, b_kind, b_exp;
-  int ee_on = 0, ee_npoly = 0, en_on = 0, nn_on = 0, pot_kind = 0;
-  double ee_kappa = 0, cusp_anti = 0.5, cusp_para = 0.25, omega = 0;
-  int P = 0;
-  std::vector<double> theta;
-  SysParams<double> sp64;
-  SysParams<float> sp32;
-  const KernelSetT<double>* k64 = nullptr;
-  const KernelSetT<float>* k32 = nullptr;
-  const NnKernelSetT<double>* nk64 = nullptr;  // neural systems
-  const NnKernelSetT<float>* nk32 = nullptr;
-  double* d_nn_theta = nullptr;  // device copy of the network parameters
-  int refs = 1;
-  bool closed = false;
-};
-
-struct mole_walkers {
-  mole_system* sys = nullptr;
-  int W = 0;
-  uint64_t seed = 0;
-  uint64_t step = 0;
-  double* pos = nullptr;  // SoA [3N][W]
-  // DMC state (allocated on first DMC call)
-  double *pos2 = nullptr, *eloc = nullptr, *eloc2 = nullptr, *weight = nullptr, *cum = nullptr, *btot = nullptr;
-  double *e_ref = nullptr, *energies = nullptr;
-  size_t energies_n = 0;
-  uint64_t* dstep = nullptr;
-  CombState* comb = nullptr;
-  bool eloc_valid = false;
-  // many-parameter SR (allocated on first use)
-  SrLargeState* srl = nullptr;
-  CUtensorMap* srl_map = nullptr;
-  double* srl_eval = nullptr;  // eval outputs: lnpsi, sign, lap, grad, O[W][8]
-};
 
 namespace {
 
@@ -203,6 +132,9 @@ cudaError_t rebuild(mole_system& s) {
 }
 
 int grid_for(int W) { return (W + kBlock - 1) / kBlock; }
+
+constexpr const char* kNoSingleKernels =
+    "no single-system kernels for this (n_up, n_dn) (compiled: 1+0, 1+1, 2+1, 2+2); run it in a mole_batch";
 
 // Kernel selection: neural systems use the network kernels (no in-kernel SR
 // sums), the others the family's kernels with or without the e-n term.
@@ -305,6 +237,13 @@ static void release_sys(mole_system* s) {
   release_ctx(c);
 }
 
+}  // extern "C"
+
+void mole::system_retain(mole_system* s) { s->refs += 1; }
+void mole::system_release(mole_system* s) { release_sys(s); }
+
+extern "C" {
+
 int mole_ctx_destroy(mole_ctx* c) {
   if (!c || c->closed) return MOLE_OK;
   c->closed = true;
@@ -328,7 +267,7 @@ int mole_sync(mole_ctx* c) {
 int mole_ctx_enable_timing(mole_ctx* c, int32_t on) {
   if (!c) return fail(MOLE_ERR_INVALID_ARG, "ctx is NULL");
   c->timing = on != 0;
-  for (int k = 0; k < 4; ++k) {
+  for (int k = 0; k < kTimeSlots; ++k) {
     c->kernel_ms[k] = 0;
     c->kernel_launches[k] = 0;
   }
@@ -336,9 +275,20 @@ int mole_ctx_enable_timing(mole_ctx* c, int32_t on) {
 }
 
 int mole_ctx_kernel_time(mole_ctx* c, int32_t kernel, double* total_ms, int64_t* launches) {
-  if (!c || kernel < 0 || kernel > 3) return fail(MOLE_ERR_INVALID_ARG, "bad ctx or kernel id");
+  if (!c || kernel < 0 || kernel >= kTimeSlots) return fail(MOLE_ERR_INVALID_ARG, "bad ctx or kernel id");
   if (total_ms) *total_ms = c->kernel_ms[kernel];
   if (launches) *launches = c->kernel_launches[kernel];
+  return MOLE_OK;
+}
+
+int mole_ctx_device_info(mole_ctx* c, int32_t* n_sm, int32_t* cc_major, int32_t* cc_minor) {
+  if (!c) return fail(MOLE_ERR_INVALID_ARG, "ctx is NULL");
+  int ma = 0, mi = 0;
+  CUDA_TRY(cudaDeviceGetAttribute(&ma, cudaDevAttrComputeCapabilityMajor, c->device));
+  CUDA_TRY(cudaDeviceGetAttribute(&mi, cudaDevAttrComputeCapabilityMinor, c->device));
+  if (n_sm) *n_sm = c->n_sm;
+  if (cc_major) *cc_major = ma;
+  if (cc_minor) *cc_minor = mi;
   return MOLE_OK;
 }
 
@@ -426,12 +376,9 @@ int mole_system_create(mole_ctx* ctx, const mole_system_desc* d, const double* t
     return fail(MOLE_ERR_SHAPE, "theta must hold " + std::to_string(P) + " parameters");
   }
   s->theta.assign(theta, theta + n_theta);
+  // spin blocks without fixed-size kernels (up to 5 + 5) run in batches only
   s->k64 = kernel_set64(s->n_up, s->n_dn);
   s->k32 = kernel_set32(s->n_up, s->n_dn);
-  if (!s->k64 || !s->k32) {
-    delete s;
-    return fail(MOLE_ERR_UNSUPPORTED, "no compiled kernels for this (n_up, n_dn); supported: n_dn = n_up or n_up - 1");
-  }
   if (s->nn_on) {
     s->nk64 = nn_kernels_f64_2_2();
     s->nk32 = nn_kernels_f32_2_2();
@@ -482,6 +429,7 @@ int mole_params_set(mole_system* s, const double* theta, int32_t n) {
   if (!s || !theta) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
   if (n != s->P) return fail(MOLE_ERR_SHAPE, "parameter count mismatch");
   s->theta.assign(theta, theta + n);
+  s->version += 1;
   CUDA_TRY(rebuild(*s));
   return MOLE_OK;
 }
@@ -609,6 +557,7 @@ int mole_eval(mole_walkers* w, int32_t precision, double* lnpsi, double* sign, d
   if (!w) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
   mole_system* s = w->sys;
   mole_ctx* c = s->ctx;
+  if (!s->nn_on && (!s->k64 || !s->k32)) return fail(MOLE_ERR_UNSUPPORTED, kNoSingleKernels);
   const int W = w->W, N = s->n_up + s->n_dn, P = s->P;
   const int nwalker_par = s->nn_on ? P - kNnP : P;
   if (nwalker_par > 8 && O) return fail(MOLE_ERR_UNSUPPORTED, "O_k output supports at most 8 orbital/Pade parameters");
@@ -656,6 +605,7 @@ int mole_vmc_run(mole_walkers* w, const mole_vmc_opts* o, double* moments, doubl
   if (!w || !o || !moments) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
   mole_system* s = w->sys;
   mole_ctx* c = s->ctx;
+  if (!s->nn_on && (!s->k64 || !s->k32)) return fail(MOLE_ERR_UNSUPPORTED, kNoSingleKernels);
   if (o->block_size < 1 || o->n_steps < 0 || o->n_eq < 0 || o->n_steps % o->block_size != 0)
     return fail(MOLE_ERR_SHAPE, "n_steps must be a non-negative multiple of block_size >= 1");
   if (o->move < MOLE_MOVE_BOX || o->move > MOLE_MOVE_DIFFUSE || !(o->step > 0.0))
@@ -761,6 +711,7 @@ int mole_vmc_run_noalloc(const mole_system* s, double* d_pos, int32_t W, uint64_
                          const mole_vmc_opts* o, double* d_moments, double* d_time_blocks, double* d_sr,
                          void* stream) {
   if (!s || !d_pos || !o || !d_moments) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
+  if (!s->nn_on && (!s->k64 || !s->k32)) return fail(MOLE_ERR_UNSUPPORTED, kNoSingleKernels);
   if (W < 1) return fail(MOLE_ERR_SHAPE, "need at least one walker");
   if (o->block_size < 1 || o->n_steps < 0 || o->n_eq < 0 || o->n_steps % o->block_size != 0)
     return fail(MOLE_ERR_SHAPE, "n_steps must be a non-negative multiple of block_size >= 1");
@@ -900,6 +851,7 @@ int mole_sr_collect_sample(mole_walkers* w, int32_t precision) {
   mole_ctx* c = s->ctx;
   SrLargeState* t = w->srl;
   if (t->finalized) return fail(MOLE_ERR_EMPTY_CACHE, "S was finalised; call mole_sr_collect_begin again");
+  if (!s->nn_on && (!s->k64 || !s->k32)) return fail(MOLE_ERR_UNSUPPORTED, kNoSingleKernels);
   const int W = w->W, N = s->n_up + s->n_dn, P = s->P;
   const int nwalker_par = s->nn_on ? P - kNnP : P;
   if (nwalker_par > 8) return fail(MOLE_ERR_UNSUPPORTED, "more than 8 orbital/Pade parameters");
@@ -1061,6 +1013,7 @@ int mole_dmc_run(mole_walkers* w, const mole_dmc_opts* o, double* energies, doub
   if (o->n_steps < 1 || !(o->tau > 0.0)) return fail(MOLE_ERR_SHAPE, "need n_steps >= 1 and tau > 0");
   mole_system* s = w->sys;
   mole_ctx* c = s->ctx;
+  if (!s->nn_on && (!s->k64 || !s->k32)) return fail(MOLE_ERR_UNSUPPORTED, kNoSingleKernels);
   const bool mixed = o->precision == MOLE_PREC_MIXED;
   if (mixed ? !dmc32(s) : !dmc64(s))
     return fail(MOLE_ERR_UNSUPPORTED, "DMC kernels are compiled for up to four electrons");
