@@ -45,7 +45,7 @@ def parse():
     p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     p.add_argument("--no-extras", action="store_true", help="skip the e2e, mixed and CPU-baseline legs")
     p.add_argument("--no-clocks", action="store_true", help="do not sample nvidia-smi during the timed region")
-    p.add_argument("--case", default=None, choices=["h2-vmc", "lih-nn-vmc", "sgemm", "be-dmc"],
+    p.add_argument("--case", default=None, choices=["h2-vmc", "lih-nn-vmc", "sgemm", "be-dmc", "ragged-batch"],
                    help="run one small kernel case (for profiling) and exit")
     return p.parse_args()
 
@@ -79,6 +79,12 @@ def run_case(case: str) -> None:
                 wk.sr_collect_sample(api.PREC_MIXED)
             wk.sr_collect_solve(1e-3, 0.05)
             r = None
+    elif case == "ragged-batch":
+        systems, walkers, widths = api.ragged_batch(64, w_range=(256, 1024))
+        b = api.Batch(ctx, systems, walkers, widths=widths)
+        b.tile = 64
+        b.run(api.MetropolisGaussian(1.0), 5, 0, 1)
+        r = [x.energy for x in b.run(api.MetropolisGaussian(1.0), 0, 20, 10)]
     else:  # be-dmc
         wf = api.WaveFunction(ctx, S.beryllium())
         wk = api.Walkers(wf, 131072)

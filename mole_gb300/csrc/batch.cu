@@ -93,7 +93,8 @@ struct mole_batch {
   int S = 0;
   int64_t walkers = 0;
   long long pos_total = 0;
-  int max_slots = 0;
+  int max_slots64 = 0, max_slots32 = 0;
+  int max_elec = 0;
   double* pos = nullptr;
   SysParams<double>* d64 = nullptr;
   SysParams<float>* d32 = nullptr;
@@ -199,7 +200,8 @@ int occupancy(bool mixed, int move, int wpb, size_t smem) {
 
 LaunchPlan plan(const mole_batch* b, bool mixed, int move, int wpb) {
   LaunchPlan p;
-  p.smem = mixed ? batch_smem_bytes<float>(wpb, b->max_slots) : batch_smem_bytes<double>(wpb, b->max_slots);
+  p.smem = mixed ? batch_smem_bytes<float>(wpb, b->max_slots32, b->max_elec)
+                 : batch_smem_bytes<double>(wpb, b->max_slots64, b->max_elec);
   const int occ = occupancy(mixed, move, wpb, p.smem);
   p.grid = std::min(b->ctx->n_sm * occ, b->n_items);
   return p;
@@ -222,7 +224,8 @@ BatchArgs make_args(const mole_batch* b, const mole_vmc_opts* o, double* pos, ui
   a.order = b->order.p;
   a.n_items = b->n_items;
   a.n_systems = b->S;
-  a.slots = b->max_slots;
+  a.slots = mixed ? b->max_slots32 : b->max_slots64;
+  a.rslots = mixed ? batch_rslots<float>(b->max_elec) : 0;
   a.pos = pos;
   a.move = o->move;
   a.n_eq = o->n_eq;
@@ -320,7 +323,9 @@ int mole_batch_create(mole_ctx* ctx, int32_t n, mole_system* const* systems, con
     b->widths[k] = in.step;
     off += (long long)3 * (in.nu + in.nd) * in.W;
     b->walkers += in.W;
-    b->max_slots = std::max(b->max_slots, batch_slots(in.nu, in.nd));
+    b->max_slots64 = std::max(b->max_slots64, batch_slots<double>(in.nu, in.nd));
+    b->max_slots32 = std::max(b->max_slots32, batch_slots<float>(in.nu, in.nd));
+    b->max_elec = std::max(b->max_elec, in.nu + in.nd);
   }
   b->pos_total = off;
   cudaError_t e = cudaMalloc(&b->pos, sizeof(double) * (size_t)off);

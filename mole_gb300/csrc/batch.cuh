@@ -41,6 +41,7 @@ struct BatchArgs {
   const int* order;         // [n_items] item ids in dispatch order
   int n_items, n_systems;
   int slots;                // doubles of walker state per thread (max over the systems)
+  int rslots;               // R-typed position shadow per thread (3 N max; 0 when R is double)
   double* pos;              // every system's SoA block
   int move, n_eq, n_steps, block_size, refresh;
   uint64_t* step0;          // device sweep counter (the random-stream position)
@@ -50,17 +51,37 @@ struct BatchArgs {
   int* status;              // bit 0: non-finite E_L; bit 1: singular determinant
 };
 
-// Shared-memory bytes of one CTA: the system image, `slots` doubles per walker
-// and the reduction scratch.
+// Shared-memory bytes of one CTA: the system image, `slots` doubles per
+// walker, the reduction scratch and, in the FP32 form, an FP32 copy of the
+// positions (`rslots` floats per walker) so that distances never pass
+// through the FP64 pipe.
 template <class R>
 __host__ __device__ constexpr size_t batch_sp_bytes() {
   return (sizeof(SysParams<R>) + 15) / 16 * 16;
 }
 template <class R>
-__host__ __device__ inline size_t batch_smem_bytes(int wpb, int slots) {
-  return batch_sp_bytes<R>() + (size_t)slots * wpb * sizeof(double) + (size_t)kNMom * (wpb / 32) * sizeof(double);
+__host__ __device__ inline int batch_rslots(int max_elec) {
+  return sizeof(R) == sizeof(double) ? 0 : 3 * max_elec;
 }
-__host__ __device__ inline int batch_slots(int nu, int nd) { return 3 * (nu + nd) + nu * nu + nd * nd; }
+template <class R>
+__host__ __device__ inline size_t batch_smem_bytes(int wpb, int slots, int max_elec) {
+  return batch_sp_bytes<R>() + (size_t)slots * wpb * sizeof(double) + (size_t)kNMom * (wpb / 32) * sizeof(double) +
+         (size_t)batch_rslots<R>(max_elec) * wpb * sizeof(R);
+}
+// FP64 slots per walker: the positions (FP64 form only; the FP32 form keeps
+// its FP64 positions in the global buffer and touches them only on accepted
+// moves) and the two inverse matrices.
+template <class R>
+__host__ __device__ inline int batch_slots(int nu, int nd) {
+  return (sizeof(R) == sizeof(double) ? 3 * (nu + nd) : 0) + nu * nu + nd * nd;
+}
+
+// a / b: IEEE in FP64, the SFU reciprocal (2 ulp) in the FP32 form.
+template <class R>
+__device__ __forceinline__ R div_t(R a, R b) {
+  if constexpr (sizeof(R) == sizeof(double)) return a / b;
+  else return __fdividef(a, b);
+}
 
 // Orbital values of spin block `spin` at r (the first kMaxSpin orbitals; the
 // unused ones have zero coefficients) and the e-n Jastrow value.
@@ -90,7 +111,7 @@ __device__ __forceinline__ void batch_orbitals(const SysParams<R>& sp, int spin,
 #pragma unroll
       for (int k = 0; k < kMaxSpin; ++k) phi[k] += sp.coef[spin][k][b] * chi;
     }
-    if (sp.en_on) jen += sp.en_coef[I] * rr / ((R)1 + sp.en_a * rr);
+    if (sp.en_on) jen += div_t<R>(sp.en_coef[I] * rr, (R)1 + sp.en_a * rr);
   }
 }
 
@@ -102,7 +123,7 @@ __device__ __forceinline__ R batch_jen(const SysParams<R>& sp, const R (&r)[3]) 
     const R d0 = r[0] - sp.nuc_pos[3 * I], d1 = r[1] - sp.nuc_pos[3 * I + 1], d2 = r[2] - sp.nuc_pos[3 * I + 2];
     const R r2 = d0 * d0 + d1 * d1 + d2 * d2;
     const R rr = r2 * rsqrt_t<R>(r2);
-    j += sp.en_coef[I] * rr / ((R)1 + sp.en_a * rr);
+    j += div_t<R>(sp.en_coef[I] * rr, (R)1 + sp.en_a * rr);
   }
   return j;
 }
@@ -114,8 +135,8 @@ __device__ __forceinline__ R batch_pair_u(const SysParams<R>& sp, bool same, R d
   const R r2 = d0 * d0 + d1 * d1 + d2 * d2;
   const R r = r2 * rsqrt_t<R>(r2);
   R Rs = r;
-  if (sp.ee_kappa > (R)0) Rs = ((R)1 - exp_t<R>(-sp.ee_kappa * r)) / sp.ee_kappa;
-  R val = (same ? sp.cusp_para : sp.cusp_anti) * Rs / ((R)1 + sp.ee_b * Rs);
+  if (sp.ee_kappa > (R)0) Rs = div_t<R>((R)1 - exp_t<R>(-sp.ee_kappa * r), sp.ee_kappa);
+  R val = div_t<R>((same ? sp.cusp_para : sp.cusp_anti) * Rs, (R)1 + sp.ee_b * Rs);
   R Rk = Rs * Rs;
   for (int i = 0; i < sp.ee_npoly; ++i) {
     val += sp.ee_poly[i] * Rk;
@@ -125,12 +146,20 @@ __device__ __forceinline__ R batch_pair_u(const SysParams<R>& sp, bool same, R d
 }
 
 // Walker view: the thread's slots in the CTA's shared state.
+template <class R>
 struct BatchWalker {
-  double* X;   // X[(3e + c) * nt]
+  double* X;   // X[(3e + c) * xs]: the FP64 positions the moves accumulate into
+               // (shared slots in the FP64 form, the global SoA buffer in the FP32 form)
+  R* Xr;       // the positions in the arithmetic type (X itself when R is double)
   double* Bu;  // inverse of the up Slater matrix, Bu[(k * nu + j) * nt]
   double* Bd;  // inverse of the down Slater matrix
-  int nt, nu, nd;
-  __device__ __forceinline__ double& x(int e, int c) const { return X[(3 * e + c) * nt]; }
+  int nt, xs, nu, nd;
+  __device__ __forceinline__ double& x(int e, int c) const { return X[(size_t)(3 * e + c) * xs]; }
+  __device__ __forceinline__ R xr(int e, int c) const { return Xr[(3 * e + c) * nt]; }
+  __device__ __forceinline__ void set_x(int e, int c, double v) const {
+    X[(size_t)(3 * e + c) * xs] = v;
+    if constexpr (sizeof(R) != sizeof(double)) Xr[(3 * e + c) * nt] = (R)v;
+  }
   __device__ __forceinline__ double* B(int spin) const { return spin ? Bd : Bu; }
 };
 
@@ -138,7 +167,7 @@ struct BatchWalker {
 // elimination with partial pivoting (the matrix in registers, padded to
 // kMaxSpin x kMaxSpin; the inverse written straight to the shared slots).
 template <class R>
-__device__ bool batch_refresh(const SysParams<R>& sp, const BatchWalker& wk) {
+__device__ bool batch_refresh(const SysParams<R>& sp, const BatchWalker<R>& wk) {
   bool ok = true;
   for (int spin = 0; spin < 2; ++spin) {
     const int n = spin ? wk.nd : wk.nu;
@@ -150,7 +179,7 @@ __device__ bool batch_refresh(const SysParams<R>& sp, const BatchWalker& wk) {
 #pragma unroll
     for (int i = 0; i < kMaxSpin; ++i) {
       if (i < n) {
-        const R r[3] = {(R)wk.x(e0 + i, 0), (R)wk.x(e0 + i, 1), (R)wk.x(e0 + i, 2)};
+        const R r[3] = {wk.xr(e0 + i, 0), wk.xr(e0 + i, 1), wk.xr(e0 + i, 2)};
         R phi[kMaxSpin], jen;
         batch_orbitals<R>(sp, spin, r, phi, jen);
 #pragma unroll
@@ -210,7 +239,7 @@ __device__ bool batch_refresh(const SysParams<R>& sp, const BatchWalker& wk) {
 // One Metropolis move of electron e (box or Gaussian, the random streams of
 // Walker::move); returns 1 when accepted.
 template <class R, int MOVE>
-__device__ __forceinline__ int batch_move(const SysParams<R>& sp, const BatchWalker& wk, int e, R step,
+__device__ __forceinline__ int batch_move(const SysParams<R>& sp, const BatchWalker<R>& wk, int e, R step,
                                           uint64_t seed, uint32_t wid, uint32_t t) {
   const int N = wk.nu + wk.nd;
   const int spin = e < wk.nu ? 0 : 1;
@@ -219,28 +248,41 @@ __device__ __forceinline__ int batch_move(const SysParams<R>& sp, const BatchWal
   const double* B = wk.B(spin);
   const int nt = wk.nt;
 
+  constexpr bool F64 = sizeof(R) == sizeof(double);
   const uint4 ra = draw4(seed, wid, t, 2u * e, kTagMove);
-  double dx[3];
+  R dx[3];  // in the FP32 form the move is made on the FP32 copy; FP64 only on acceptance
   R uacc;
+  float z[3];
   if constexpr (MOVE == kMoveBox) {
-    dx[0] = (double)(step * (u01<R>(ra.x) - (R)0.5));
-    dx[1] = (double)(step * (u01<R>(ra.y) - (R)0.5));
-    dx[2] = (double)(step * (u01<R>(ra.z) - (R)0.5));
+    dx[0] = step * (u01<R>(ra.x) - (R)0.5);
+    dx[1] = step * (u01<R>(ra.y) - (R)0.5);
+    dx[2] = step * (u01<R>(ra.z) - (R)0.5);
     uacc = u01<R>(ra.w);
   } else {
-    float z0, z1, z2, z3;
-    repro_box_muller(ra.x, ra.y, z0, z1);
-    repro_box_muller(ra.z, ra.w, z2, z3);
+    float z3;
+    repro_box_muller(ra.x, ra.y, z[0], z[1]);
+    repro_box_muller(ra.z, ra.w, z[2], z3);
     const uint4 rb = draw4(seed, wid, t, 2u * e + 1u, kTagMove);
     uacc = u01<R>(rb.x);
-    dx[0] = (double)step * (double)z0;
-    dx[1] = (double)step * (double)z1;
-    dx[2] = (double)step * (double)z2;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) dx[c] = step * (R)z[c];
   }
-  const double xo[3] = {wk.x(e, 0), wk.x(e, 1), wk.x(e, 2)};
-  const double xn[3] = {xo[0] + dx[0], xo[1] + dx[1], xo[2] + dx[2]};
-  const R rn[3] = {(R)xn[0], (R)xn[1], (R)xn[2]};
-  const R ro[3] = {(R)xo[0], (R)xo[1], (R)xo[2]};
+  const R ro[3] = {wk.xr(e, 0), wk.xr(e, 1), wk.xr(e, 2)};
+  R rn[3];
+  double xn[3];
+  if constexpr (F64) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      xn[c] = ro[c] + (double)dx[c];
+      rn[c] = xn[c];
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      rn[c] = ro[c] + dx[c];
+      xn[c] = wk.x(e, c);  // global load, consumed only if the move is accepted
+    }
+  }
   R phi[kMaxSpin], jn;
   batch_orbitals<R>(sp, spin, rn, phi, jn);
   const R jo = sp.en_on ? batch_jen<R>(sp, ro) : (R)0;
@@ -252,17 +294,26 @@ __device__ __forceinline__ int batch_move(const SysParams<R>& sp, const BatchWal
   for (int j = 0; j < N; ++j) {
     if (j == e) continue;
     const bool same = (j < wk.nu) == (spin == 0);
-    const R xj[3] = {(R)wk.x(j, 0), (R)wk.x(j, 1), (R)wk.x(j, 2)};
+    const R xj[3] = {wk.xr(j, 0), wk.xr(j, 1), wk.xr(j, 2)};
     dJ += batch_pair_u<R>(sp, same, rn[0] - xj[0], rn[1] - xj[1], rn[2] - xj[2]) -
-          batch_pair_u<R>(sp, same, (R)(xo[0] - wk.x(j, 0)), (R)(xo[1] - wk.x(j, 1)), (R)(xo[2] - wk.x(j, 2)));
+          batch_pair_u<R>(sp, same, ro[0] - xj[0], ro[1] - xj[1], ro[2] - xj[2]);
   }
-  const double p = ratio * ratio * (double)exp_t<R>((R)2 * dJ);
-  if (!(p > (double)uacc)) return 0;
+  if constexpr (F64) {
+    const double p = ratio * ratio * exp(2.0 * dJ);
+    if (!(p > uacc)) return 0;
+  } else {
+    const float rf = (float)ratio;  // the acceptance test itself is a random comparison: FP32
+    if (!(rf * rf * __expf(2.0f * dJ) > uacc)) return 0;
+  }
 
   // commit: position and the FP64 Sherman-Morrison row update
-  wk.x(e, 0) = xn[0];
-  wk.x(e, 1) = xn[1];
-  wk.x(e, 2) = xn[2];
+  if constexpr (F64) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) wk.set_x(e, c, xn[c]);
+  } else {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) wk.set_x(e, c, xn[c] + (double)dx[c]);
+  }
   double v[kMaxSpin], col[kMaxSpin];
   double* Bw = wk.B(spin);
 #pragma unroll
@@ -292,7 +343,7 @@ __device__ __forceinline__ int batch_move(const SysParams<R>& sp, const BatchWal
 // gradients and Laplacians in R contracted with the FP64 inverse, Jastrow and
 // potential terms re-evaluated per electron (each pair from both sides).
 template <class R>
-__device__ double batch_local_energy(const SysParams<R>& sp, const BatchWalker& wk) {
+__device__ double batch_local_energy(const SysParams<R>& sp, const BatchWalker<R>& wk) {
   const int N = wk.nu + wk.nd;
   const int nt = wk.nt;
   double lap = 0.0, V = sp.vnn;
@@ -301,7 +352,7 @@ __device__ double batch_local_energy(const SysParams<R>& sp, const BatchWalker& 
     const int n = spin ? wk.nd : wk.nu;
     const int i = spin ? e - wk.nu : e;
     const double* B = wk.B(spin);
-    const R r[3] = {(R)wk.x(e, 0), (R)wk.x(e, 1), (R)wk.x(e, 2)};
+    const R r[3] = {wk.xr(e, 0), wk.xr(e, 1), wk.xr(e, 2)};
     OneBody<R, kMaxSpin, 0> o;
     one_body<R, kMaxSpin, 0, true, false>(sp, spin, r, o);
     double gD[3] = {0.0, 0.0, 0.0}, lD = 0.0;
@@ -315,26 +366,23 @@ __device__ double batch_local_energy(const SysParams<R>& sp, const BatchWalker& 
         lD += (double)o.lap[k] * b;
       }
     R gJ[3] = {o.gjen[0], o.gjen[1], o.gjen[2]};
-    R lJ = o.ljen;
+    R lJ = o.ljen, Ve = o.ven;
     for (int j = 0; j < N; ++j) {
       if (j == e) continue;
-      const R d0 = (R)(wk.x(e, 0) - wk.x(j, 0)), d1 = (R)(wk.x(e, 1) - wk.x(j, 1)), d2 = (R)(wk.x(e, 2) - wk.x(j, 2));
+      const R d0 = r[0] - wk.xr(j, 0), d1 = r[1] - wk.xr(j, 1), d2 = r[2] - wk.xr(j, 2);
       PairVals<R, 0> pv;
       pair_vals<R, 0, false>(sp, (j < wk.nu) == (spin == 0), d0, d1, d2, pv);
       gJ[0] += pv.f * d0;
       gJ[1] += pv.f * d1;
       gJ[2] += pv.f * d2;
       lJ += pv.l;
-      if (j > e) V += (double)pv.inv;
+      if (j > e) Ve += pv.inv;
     }
-    double dot = 0.0, gj2 = 0.0;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      dot += gD[c] * (double)gJ[c];
-      gj2 += (double)gJ[c] * (double)gJ[c];
-    }
-    lap += lD + (double)lJ + 2.0 * dot + gj2;
-    V += (double)o.ven;
+    // the electron's Jastrow-only terms in R, the determinant terms in FP64
+    const R jj = lJ + gJ[0] * gJ[0] + gJ[1] * gJ[1] + gJ[2] * gJ[2];
+    const double dot = gD[0] * (double)gJ[0] + gD[1] * (double)gJ[1] + gD[2] * (double)gJ[2];
+    lap += lD + (double)jj + 2.0 * dot;
+    V += (double)Ve;
   }
   return -0.5 * lap + V;
 }
@@ -348,17 +396,31 @@ __device__ void batch_item(const SysParams<R>& sp, const BatchSystem& bs, int id
   const int w = w0 + tid;
   const bool active = w < bs.W;
   const int N = bs.nu + bs.nd;
-  BatchWalker wk;
+  constexpr bool F64 = sizeof(R) == sizeof(double);
+  double* gp = a.pos + bs.pos_off;
+  BatchWalker<R> wk;
   wk.nt = nt;
   wk.nu = bs.nu;
   wk.nd = bs.nd;
-  wk.X = st + tid;
-  wk.Bu = wk.X + (size_t)3 * N * nt;
+  if constexpr (F64) {
+    wk.X = st + tid;
+    wk.xs = nt;
+    wk.Bu = wk.X + (size_t)3 * N * nt;
+    wk.Xr = reinterpret_cast<R*>(wk.X);
+  } else {
+    wk.X = gp + (active ? w : 0);
+    wk.xs = bs.W;
+    wk.Bu = st + tid;
+    wk.Xr = reinterpret_cast<R*>(st + (size_t)a.slots * nt + (size_t)kNMom * (nt / 32)) + tid;
+  }
   wk.Bd = wk.Bu + (size_t)bs.nu * bs.nu * nt;
   double acc[kNMom] = {0, 0, 0, 0, 0, 0, 0};
   if (active) {
-    double* gp = a.pos + bs.pos_off;
-    for (int k = 0; k < 3 * N; ++k) wk.X[k * nt] = gp[(size_t)k * bs.W + w];
+    for (int k = 0; k < 3 * N; ++k) {
+      const double v = gp[(size_t)k * bs.W + w];
+      if constexpr (F64) wk.X[k * nt] = v;
+      else wk.Xr[k * nt] = (R)v;
+    }
     bool ok = batch_refresh<R>(sp, wk);
     const int total = a.n_eq + a.n_steps;
     const int refresh = a.refresh > 0 ? a.refresh : 100;
@@ -380,7 +442,8 @@ __device__ void batch_item(const SysParams<R>& sp, const BatchSystem& bs, int id
         bsum = 0.0;
       }
     }
-    for (int k = 0; k < 3 * N; ++k) gp[(size_t)k * bs.W + w] = wk.X[k * nt];
+    if constexpr (F64)
+      for (int k = 0; k < 3 * N; ++k) gp[(size_t)k * bs.W + w] = wk.X[k * nt];
     if (!ok) atomicOr(a.status, 2);
     if (!(sE == sE) || !(sE2 < 1e300)) atomicOr(a.status, 1);
     acc[0] = (double)a.n_steps;
