@@ -225,6 +225,119 @@ def lih_time_to_sigma(ctx, W: int, train_iters: int, target: float = 1e-3) -> di
     return out
 
 
+def cpu_batch_sample(systems, walkers, widths, threads: int, target_s: float = 12.0) -> dict:
+    """The CPU oracle's VMC (dense determinants and every term recomputed at
+    every move, as the reference's call pattern recomputes psi) over a
+    bounded sample of the ragged batch: 64 walkers of each system, systems
+    taken in order, 20 sweeps each, on `threads` host threads (ctypes
+    releases the interpreter lock), until about target_s seconds."""
+    import concurrent.futures as cf
+
+    import numpy as np
+
+    from mole_gb300.system import MOVE_GAUSS
+    from oracle import oracle as O
+
+    O.build()
+    sweeps, W = 20, 64
+
+    def one(k):
+        s = systems[k]
+        pos = O.init_positions(W, s.n_elec, 0x5EED + k)
+        O.vmc_run(s, pos, move=MOVE_GAUSS, step=float(widths[k]), n_eq=0, n_steps=sweeps, block_size=sweeps,
+                  seed=0x5EED + k)
+        return W * sweeps
+
+    done, k = 0, 0
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        while time.perf_counter() - t0 < target_s:
+            futs = [ex.submit(one, (k + j) % len(systems)) for j in range(threads)]
+            done += sum(f.result() for f in futs)
+            k += threads
+    secs = time.perf_counter() - t0
+    return {"value": done / secs, "unit": "walker-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{done // (W * sweeps)} systems x {W} walkers x {sweeps} sweeps ({secs:.1f} s), CPU oracle "
+                      "(dense determinants, psi recomputed at every move), one thread per system"}
+
+
+def ragged_batch_leg(ctx, steps: int, sweeps: int = 100) -> dict:
+    """The ragged batch: 256 atoms/ions (Z in U{2..10}, N in U{2..10},
+    1s/2s/2p STOs, Pade e-e and e-n Jastrows), walkers U{256..4096} each, one
+    persistent launch per graph replay (a replay = `sweeps` sweeps with E_L
+    every sweep), tile chosen by the autotuner. The FP32-evaluation form is
+    the timed one; the FP64 form runs alongside. The energy error of the
+    mixed form against FP64 is given two ways: E_L at identical positions
+    (the evaluation error alone) and the per-system energies of independent
+    runs (z = |dE| / combined blocking error)."""
+    import numpy as np
+
+    from mole_gb300 import api, flop_model
+
+    systems, W, widths = api.ragged_batch(256)
+    out = {"workload": "256 atoms/ions, Z in U{2..10}, N in U{2..10}, walkers U{256..4096}, Gaussian moves "
+                       "0.6/sqrt(Z) bohr, E_L every sweep, FP64 inverse refresh every 100 sweeps",
+           "systems": len(systems), "walkers": int(W.sum()), "sweeps_per_replay": sweeps}
+    res, batches = {}, {}
+    mv = api.MetropolisGaussian(1.0)
+    for prec in (api.PREC_MIXED, api.PREC_FP64):
+        b = api.Batch(ctx, systems, W, widths=widths)
+        tune = b.autotune(mv, prec, sweeps=10, cache=False)
+        b.run(mv, 1000 if prec == api.PREC_MIXED else 300, 0, 1, precision=prec)  # equilibration
+        n_rep = max(steps, 10) if prec == api.PREC_MIXED else 4
+        ctx.enable_timing(True)
+        torch_sync()
+        t0 = time.perf_counter()
+        rs = [b.run(mv, 0, sweeps, 50, precision=prec) for _ in range(n_rep)]
+        wall = time.perf_counter() - t0
+        ms, n = ctx.kernel_time(4)
+        ctx.enable_timing(False)
+        mom = np.sum([[r.moments for r in rep] for rep in rs], axis=0)
+        E = mom[:, 1] / mom[:, 0]
+        err = np.array([api.blocking_error(m) for m in mom])
+        acc = mom[:, 5] / mom[:, 6]
+        fp64 = sum(int(W[k]) * flop_model.batch_step_fp64(s.n_up, s.n_dn, float(acc[k])).flops
+                   for k, s in enumerate(systems)) * sweeps
+        res[prec] = {"value": float(W.sum()) * sweeps * n / (ms * 1e-3), "unit": "walker-steps/s",
+                     "ms_per_replay": ms / n, "wall_ms_per_replay": 1e3 * wall / n_rep, "tile": b.tile,
+                     "grid": b.grid(prec), "tune_ms": tune["timings"], "graph_replays": b.graph_launches,
+                     "fp64_tflops": fp64 / (ms / n * 1e-3) / 1e12, "E": E, "err": err,
+                     "acceptance": float(np.mean(acc))}
+        batches[prec] = b
+    m, f = res[api.PREC_MIXED], res[api.PREC_FP64]
+    z = np.abs(m["E"] - f["E"]) / np.hypot(m["err"], f["err"])
+    # evaluation error: the FP64 batch's positions in both, moves of 1e-12 bohr, one sampled sweep
+    for k in range(len(systems)):
+        batches[api.PREC_MIXED].set_positions(k, batches[api.PREC_FP64].positions(k))
+    ev = {prec: np.array([r.energy for r in batches[prec].run(api.MetropolisGaussian(1e-12), 0, 1, 1, precision=prec)])
+          for prec in (api.PREC_FP64, api.PREC_MIXED)}
+    rel = np.abs(ev[api.PREC_MIXED] - ev[api.PREC_FP64]) / np.maximum(np.abs(ev[api.PREC_FP64]), 1.0)
+    for b in batches.values():
+        b.close()
+    out["mixed"] = {k: v for k, v in m.items() if k not in ("E", "err")}
+    out["fp64"] = {k: v for k, v in f.items() if k not in ("E", "err")}
+    out["energy_delta_vs_fp64"] = {
+        "same_positions_rel_max": float(rel.max()), "same_positions_rel_median": float(np.median(rel)),
+        "independent_runs_frac_z_lt_2": float(np.mean(z < 2.0)), "independent_runs_frac_z_lt_3": float(np.mean(z < 3.0)),
+        "independent_runs_max_z": float(np.max(z)),
+        "note": "same_positions: mean E_L of each system at identical configurations (FP32 evaluation vs FP64); "
+                "independent_runs: per-system energies of separate chains, z = |dE| / combined blocking error "
+                "(50-sweep blocks; these trial functions violate the nuclear cusps, so E_L is heavy-tailed)"}
+    peak = ctx.probe_peaks()[0] / 1e3
+    out["roofline"] = {"bound": "fp64", "kernel": "batch_vmc_kernel<float, Gaussian>",
+                       "achieved": m["fp64_tflops"], "peak": peak, "unit": "TFLOP/s",
+                       "frac": m["fp64_tflops"] / peak,
+                       "note": "algorithmic FP64 work of the FP32-evaluation form (flop_model.batch_step_fp64); "
+                               "the FP32 orbital/Jastrow work is not counted"}
+    return out
+
+
+def torch_sync():
+    import torch
+
+    torch.cuda.synchronize()
+
+
 def run_reference(args):
     rank, world, _ = dist_info()
     if rank != 0:
@@ -299,19 +412,21 @@ def main():
         if world > 1:
             torch.distributed.barrier()
 
+    step_ms = []
+
     def timed(fn, steps):
         barrier()
         torch.cuda.synchronize()
-        t0 = torch.cuda.Event(enable_timing=True)
-        t1 = torch.cuda.Event(enable_timing=True)
-        t0.record(stream)
-        for _ in range(steps):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+        ev[0].record(stream)
+        for i in range(steps):
             flush.zero_()  # evict L2 between iterations
             fn()
-        t1.record(stream)
+            ev[i + 1].record(stream)
         torch.cuda.synchronize()
         barrier()
-        ms = t0.elapsed_time(t1)
+        step_ms[:] = [ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]
+        ms = ev[0].elapsed_time(ev[steps])
         if world > 1:
             t = torch.tensor([ms], device="cuda")
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -330,6 +445,7 @@ def main():
     host_t0 = time.perf_counter()
     ms = timed(lambda: results.append(sr_step(wf, sampler)), args.steps)
     host_s = time.perf_counter() - host_t0
+    device_step_ms = list(step_ms)
     clk = clocks.stop()
     k_ms, k_n = ctx.kernel_time(0)
     ctx.enable_timing(False)
@@ -347,7 +463,8 @@ def main():
                 "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
                 "kernel": "vmc_kernel<1,1,double,2,false>" if prec == api.PREC_FP64 else "vmc_kernel<1,1,float,2,false>",
                 "kernel_ms_per_launch": k_ms / k_n, "kernel_share_of_step": k_ms / ms,
-                "host_wall_ms_per_step": 1e3 * host_s / args.steps, "flops_per_walker_step": work.flops,
+                "host_wall_ms_per_step": 1e3 * host_s / args.steps, "step_ms": device_step_ms,
+                "flops_per_walker_step": work.flops,
                 "special_per_walker_step": work.special,
                 "peak_source": "measured live: FMA-chain probe (mole_probe_peaks)"}
 
@@ -397,14 +514,23 @@ def main():
         # -------------------------------------------------- neural vs plain, LiH
         if rank == 0 and world == 1:
             line["lih_time_to_sigma"] = lih_time_to_sigma(ctx, 16384, 20)
+        # -------------------------------------------------- ragged batch of systems
+        if rank == 0 and world == 1:
+            line["ragged_batch"] = ragged_batch_leg(ctx, max(3, args.steps // 2))
+            from oracle import oracle as O
+
+            systems, Wb, widths = __import__("mole_gb300.api", fromlist=["api"]).ragged_batch(256)
+            line["ragged_batch"]["cpu_baseline"] = cpu_batch_sample(systems, Wb, widths, O.hardware_threads())
         # -------------------------------------------------- CPU baseline
         if rank == 0 and world == 1:
             from oracle import oracle as O
 
             threads = O.hardware_threads()
-            rate, secs, _ = cpu_baseline_sample(threads, 512 * threads, 2000)
+            rate, secs, _ = cpu_baseline_sample(threads, 256 * threads, 400)  # probe, then ~12 s of work
+            wk_cpu = int(max(1, round(12.0 * rate / 2000 / threads / 64))) * 64 * threads
+            rate, secs, _ = cpu_baseline_sample(threads, wk_cpu, 2000)
             line["cpu_baseline"] = {"value": rate, "unit": "walker-steps/s", "cores": threads, "kind": "port",
-                                    "sample": f"{512 * threads} walkers x 2000 sweeps ({secs:.1f} s), reference call "
+                                    "sample": f"{wk_cpu} walkers x 2000 sweeps ({secs:.1f} s), reference call "
                                               "pattern (oracle/faithful.cpp), std::thread over all host cores"}
     if rank == 0:
         print(json.dumps(line, default=_json_default), flush=True)

@@ -106,3 +106,22 @@ def walker_step(system: System, move: int, sr_params: int = 0, acceptance: float
     # accumulation: E, E^2, blocking, O_k, E O_k, O_k O_l
     w.add(4 + 2 * sr_params + sr_params * (sr_params + 1))
     return w
+
+
+def batch_step_fp64(n_up: int, n_dn: int, acceptance: float = 0.5) -> Work:
+    """FP64 arithmetic of one walker-step of the ragged-batch kernel in its
+    FP32-evaluation form (mole_gb300/csrc/batch.cuh): per move the
+    determinant ratio (n products), on acceptance the Sherman-Morrison
+    row update (v = phi B, B -= col v^T, one division) and the FP64 position
+    update; per electron of the local energy the gradient and Laplacian
+    contractions with the inverse (4 n products), the dot product with the
+    Jastrow gradient and the assembly. Orbital, Jastrow and potential terms
+    are FP32 work and are not counted here."""
+    w = Work()
+    for e in range(n_up + n_dn):
+        n = n_up if e < n_up else n_dn
+        w.add(2 * n)
+        w.add(acceptance * (4 * n * n + n + 3), acceptance)
+        w.add(8 * n + 6 + 4)
+    w.add(4)  # E, E^2 and blocking sums
+    return w
