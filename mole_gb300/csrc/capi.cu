@@ -117,16 +117,28 @@ void fill_params(const mole_system& s, SysParams<R>& sp) {
     }
   sp.vnn = vnn;
   sp.nn_theta = s.d_nn_theta;
+  sp.nn_tab = s.d_nn_tab;
 }
 
 // Re-derives both kernel-parameter images and, for neural systems, the
-// device copy of the network parameters (a synchronous 72 KB copy).
+// device copy of the network parameters (a synchronous 72 KB copy) and the
+// FP32 form's quintic tables (built on the context stream; the call waits for
+// them and for any earlier work that may still read the old ones).
 cudaError_t rebuild(mole_system& s) {
   fill_params(s, s.sp64);
   fill_params(s, s.sp32);
   if (s.nn_on && s.d_nn_theta) {
+    cudaStream_t st = s.ctx->stream;
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return e;
     const int off = s.n_exp + (s.ee_on ? 1 + s.ee_npoly : 0) + (s.en_on ? 1 : 0);
-    return cudaMemcpy(s.d_nn_theta, s.theta.data() + off, sizeof(double) * kNnP, cudaMemcpyHostToDevice);
+    e = cudaMemcpy(s.d_nn_theta, s.theta.data() + off, sizeof(double) * kNnP, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return e;
+    std::vector<double> z(s.n_nuc);
+    for (int I = 0; I < s.n_nuc; ++I) z[I] = (double)s.nuc_z[I];
+    e = launch_nn_tables(s.d_nn_theta, s.n_nuc, z.data(), s.d_nn_node, s.d_nn_tab, st);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(st);
   }
   return cudaSuccess;
 }
@@ -229,7 +241,9 @@ static void release_sys(mole_system* s) {
   if (--s->refs > 0) return;
   if (s->d_nn_theta) {
     cudaSetDevice(s->ctx->device);
-    cudaFree(s->d_nn_theta);
+    cudaStreamSynchronize(s->ctx->stream);
+    for (void* p : {(void*)s->d_nn_theta, (void*)s->d_nn_tab, (void*)s->d_nn_node})
+      if (p) cudaFree(p);
     cudaGetLastError();
   }
   mole_ctx* c = s->ctx;
@@ -384,15 +398,21 @@ int mole_system_create(mole_ctx* ctx, const mole_system_desc* d, const double* t
     s->nk32 = nn_kernels_f32_2_2();
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e == cudaSuccess) e = cudaMalloc(&s->d_nn_theta, sizeof(double) * kNnP);
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_nn_tab, sizeof(float) * nn_tab_floats(s->n_nuc));
+    if (e == cudaSuccess)
+      e = cudaMalloc(&s->d_nn_node, sizeof(double) * 3 * (size_t)(2 + s->n_nuc) * kNnTabNodes);
     if (e != cudaSuccess) {
+      for (void* p : {(void*)s->d_nn_theta, (void*)s->d_nn_tab, (void*)s->d_nn_node})
+        if (p) cudaFree(p);
       delete s;
       return fail(MOLE_ERR_CUDA, std::string("network parameters: ") + cudaGetErrorString(e));
     }
   }
   if (rebuild(*s) != cudaSuccess) {
-    if (s->d_nn_theta) cudaFree(s->d_nn_theta);
+    for (void* p : {(void*)s->d_nn_theta, (void*)s->d_nn_tab, (void*)s->d_nn_node})
+      if (p) cudaFree(p);
     delete s;
-    return fail(MOLE_ERR_CUDA, "copying the network parameters failed");
+    return fail(MOLE_ERR_CUDA, "copying the network parameters or building their tables failed");
   }
   ctx->refs += 1;
   *out = s;

@@ -75,12 +75,18 @@ struct NnKernelSetT {
 template <class K>
 cudaError_t nn_prepare(K kernel, size_t smem) {
   // opt in to more than 48 KB of dynamic shared memory (idempotent)
-  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  return smem ? cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) : cudaSuccess;
+}
+// The FP64 form keeps both nets and the per-thread hidden-layer jets in
+// shared memory; the FP32 form interpolates its tables and needs none.
+template <class R>
+constexpr size_t nn_launch_smem() {
+  return std::is_same<R, float>::value ? 0 : nn_smem_bytes<R>(kBlock);
 }
 template <int NU, int ND, class R, bool DRIFT>
 cudaError_t launch_vmc_nn(const SysParams<R>& sp, const VmcArgs& a, int grid, cudaStream_t s) {
   auto k = vmc_kernel<NU, ND, R, 0, DRIFT, true, true>;
-  const size_t smem = nn_smem_bytes<R>(kBlock);
+  const size_t smem = nn_launch_smem<R>();
   cudaError_t e = nn_prepare(k, smem);
   if (e != cudaSuccess) return e;
   k<<<grid, kBlock, smem, s>>>(sp, a);
@@ -89,7 +95,7 @@ cudaError_t launch_vmc_nn(const SysParams<R>& sp, const VmcArgs& a, int grid, cu
 template <int NU, int ND, class R>
 cudaError_t launch_eval_nn(const SysParams<R>& sp, const EvalArgs& a, int grid, cudaStream_t s) {
   auto k = eval_kernel<NU, ND, R, 8, true, true>;
-  const size_t smem = nn_smem_bytes<R>(kBlock);
+  const size_t smem = nn_launch_smem<R>();
   cudaError_t e = nn_prepare(k, smem);
   if (e != cudaSuccess) return e;
   k<<<grid, kBlock, smem, s>>>(sp, a);
@@ -98,7 +104,7 @@ cudaError_t launch_eval_nn(const SysParams<R>& sp, const EvalArgs& a, int grid, 
 template <int NU, int ND, class R>
 cudaError_t launch_dmc_nn(const SysParams<R>& sp, const DmcArgs& a, int grid, cudaStream_t s) {
   auto k = dmc_step_kernel<NU, ND, R, true, true>;
-  const size_t smem = nn_smem_bytes<R>(kBlock);
+  const size_t smem = nn_launch_smem<R>();
   cudaError_t e = nn_prepare(k, smem);
   if (e != cudaSuccess) return e;
   k<<<grid, kBlock, smem, s>>>(sp, a);

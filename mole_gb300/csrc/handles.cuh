@@ -76,6 +76,8 @@ struct mole_system {
   const NnKernelSetT<double>* nk64 = nullptr;  // neural systems
   const NnKernelSetT<float>* nk32 = nullptr;
   double* d_nn_theta = nullptr;  // device copy of the network parameters
+  float* d_nn_tab = nullptr;      // quintic tables of the pair networks (FP32 form)
+  double* d_nn_node = nullptr;    // FP64 node values the tables are built from
   int refs = 1;
   bool closed = false;
 };

@@ -41,7 +41,7 @@ extern __shared__ __align__(16) unsigned char mole_dyn_smem[];
 template <class R, bool NN>
 __device__ __forceinline__ NnCtx<R> nn_setup(const SysParams<R>& sp) {
   NnCtx<R> c{nullptr, nullptr, 0};
-  if constexpr (NN) {
+  if constexpr (NN && !std::is_same<R, float>::value) {  // the FP32 form reads the quintic tables instead
     auto* sh = reinterpret_cast<NnShared<R>*>(mole_dyn_smem);
     nn_load<R>(sh, sp.nn_theta);
     R* scr = reinterpret_cast<R*>(mole_dyn_smem + sizeof(NnShared<R>));

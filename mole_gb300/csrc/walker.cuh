@@ -47,6 +47,7 @@ struct SysParams {
   double vnn;  // n-n repulsion constant
   int n_exp, P, off_ee, off_en, off_nn;
   const double* nn_theta;  // device copy of the 9,090 network parameters (neural systems)
+  const float* nn_tab;     // quintic tables of the pair networks (neural systems, FP32 form)
 };
 
 template <class R>
@@ -182,7 +183,8 @@ __device__ __forceinline__ void one_body(const SysParams<R>& sp, int spin, const
     }
     if constexpr (NN) {
       R y, y1, y2;
-      nn_jet<R>(nn->sh->net[1], rr, sp.nuc_z[I], nn->scr, nn->stride, y, y1, y2);
+      if constexpr (std::is_same<R, float>::value) nn_tab_eval(sp.nn_tab, 2 + I, rr, y, y1, y2);
+      else nn_jet<R>(nn->sh->net[1], rr, sp.nuc_z[I], nn->scr, nn->stride, y, y1, y2);
       const R f = y1 * inv;
       o.jen += y;
       o.gjen[0] += f * d0;
@@ -216,7 +218,8 @@ __device__ __forceinline__ void pair_vals(const SysParams<R>& sp, bool same, R d
   v.rs = r;
   if constexpr (NN) {
     R y, y1, y2;
-    nn_jet<R>(nn->sh->net[0], r, same ? (R)1 : (R)0, nn->scr, nn->stride, y, y1, y2);
+    if constexpr (std::is_same<R, float>::value) nn_tab_eval(sp.nn_tab, same ? 0 : 1, r, y, y1, y2);
+    else nn_jet<R>(nn->sh->net[0], r, same ? (R)1 : (R)0, nn->scr, nn->stride, y, y1, y2);
     v.u = y;
     v.f = y1 * inv;
     v.l = y2 + (R)2 * v.f;
