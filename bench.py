@@ -163,7 +163,7 @@ def cpu_baseline_sample(threads: int, walkers: int, sweeps: int):
 
 
 def lih_time_to_sigma(ctx, W: int, train_iters: int, target: float = 1e-3) -> dict:
-    """LiH (configs[3] geometry): the plain form (Slater x Pade, FP64, SR over
+    """LiH (Li Z=3 at the origin, H at z = 3.015 bohr): the plain form (Slater x Pade, FP64, SR over
     the orbital exponents and b) against the neural form (network Jastrow,
     FP32 evaluation / FP64 accumulation, SR over all 9,094 parameters on the
     tensor cores), both trained from the same start; then each samples until
@@ -209,6 +209,20 @@ def lih_time_to_sigma(ctx, W: int, train_iters: int, target: float = 1e-3) -> di
         leg = {"time_to_sigma_s": secs, "sweeps": sweeps, "energy": E, "error": err,
                "variance": mom[2] / mom[0] - E * E, "walker_steps_per_s": W * sweeps / secs,
                "train_s": train_s, "train_iters": train_iters, "vmc_kernel_ms_per_launch": v_ms / max(v_n, 1)}
+        if neural:
+            # the mixed form's error against an all-FP64 run of the same network
+            ev32 = wk.evaluate(api.PREC_MIXED, want_O=False)["eloc"]
+            ev64 = wk.evaluate(api.PREC_FP64, want_O=False)["eloc"]
+            leg["energy_delta_vs_fp64"] = {
+                "same_positions_mean_ha": float(np.mean(ev32) - np.mean(ev64)),
+                "same_positions_max_abs_ha": float(np.max(np.abs(ev32 - ev64))),
+                "same_positions_median_rel": float(np.median(np.abs(ev32 - ev64) / np.abs(ev64)))}
+            s64 = api.Sampler(wf, api.MetropolisGaussian(0.3), wk, precision=api.PREC_FP64)
+            s64.run(20, 0, 1)
+            r64 = s64.run(0, 100, 10)
+            leg["energy_delta_vs_fp64"].update({"fp64_energy": r64.energy, "fp64_error": r64.error,
+                                                "note": "same network and walkers; FP64 form evaluates the "
+                                                        "MLP directly, the mixed form interpolates its tables"})
         if neural and g_n:
             P_pad = (s.n_params + 127) // 128 * 128
             flops = 2.0 * P_pad * P_pad * ((W + 63) // 64 * 64) * 0.5 * (1 + 128.0 / P_pad)  # upper tiles only
@@ -403,8 +417,12 @@ def main():
 
     sr = api.StochasticReconfiguration(0.05, 1e-3)
 
+    from mole_gb300.distributed import allreduce_result
+
     def sr_step(wf, sampler):
         r = sampler.run(0, sweeps, block, sr=True)
+        if world > 1:  # the SR iteration's one exchange: sums over every rank's walkers
+            r = allreduce_result(r)
         wf.update_parameters(sr.compute_parameter_update(wf.parameters(), r, ctx))
         return r
 

@@ -468,15 +468,23 @@ class VmcRunner:
     the optimizer's update to the wavefunction. Unlike the reference, the
     chains continue from where the previous iteration left them."""
 
-    def __init__(self, sampler: Sampler, optimizer):
+    def __init__(self, sampler: Sampler, optimizer, group=None):
         self.sampler, self.optimizer = sampler, optimizer
+        self.group = group  # torch.distributed group whose ranks split the walkers (None: all ranks)
 
     def run_optimization(self, iters: int, steps: int, block_size: int, callback=None):
+        from .distributed import allreduce_result, world
+
         wf = self.sampler.wave_function()
         energies, errors, results = [], [], []
         large = wf.num_parameters() > 8
+        multi = world()[1] > 1
+        if multi and large:
+            raise MoleError(103, "the many-parameter SR path runs on one rank")
         for it in range(iters):
             r = Runner(self.sampler).run(steps, block_size, sr=not large)
+            if multi:  # every rank's sums, so every rank takes the same step
+                r = allreduce_result(r, self.group)
             energies.append(r.energy)
             errors.append(r.error)
             results.append(r)

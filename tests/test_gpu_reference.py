@@ -61,7 +61,7 @@ def test_steepest_descent_moves_downhill(ctx):
 
 
 def test_vmc_energy_statistics_fp64_vs_mixed(ctx):
-    # configs[0]-like helium: the mixed form agrees with FP64 within 2 sigma
+    # helium singlet (alpha 1.6875, beta 0.3): the mixed form agrees with FP64 within 2 sigma
     res = {}
     for prec in (api.PREC_FP64, api.PREC_MIXED):
         wf = api.WaveFunction(ctx, S.helium(1.6875, 0.3))
@@ -75,7 +75,7 @@ def test_vmc_energy_statistics_fp64_vs_mixed(ctx):
 
 
 def test_h2_sr_optimisation_lowers_energy(ctx):
-    # configs[1] at reduced size: alpha = 1.0, b = 0.5, Gaussian moves 0.4, eps 1e-3, step 0.05
+    # the H2 VMC + SR workload at reduced size: alpha = 1.0, b = 0.5, Gaussian moves 0.4, eps 1e-3, step 0.05
     wf = api.WaveFunction(ctx, S.h2(1.0, 0.5))
     wk = api.Walkers(wf, 8192)
     vmc = api.VmcRunner(api.Sampler(wf, api.MetropolisGaussian(0.4), wk), api.StochasticReconfiguration(0.05, 1e-3))
