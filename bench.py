@@ -346,6 +346,79 @@ def ragged_batch_leg(ctx, steps: int, sweeps: int = 100) -> dict:
     return out
 
 
+def dmc_leg(ctx, n_eq: int = 600, n_steps: int = 800, train_iters: int = 20) -> dict:
+    """DMC on the Be atom (Z = 4, 2 up + 2 down, 1s/2s STO determinant):
+    131,072 walkers, time step 0.005, drift-diffusion moves with Metropolis
+    accept/reject, a stochastic comb every step, FP64 weights and energy
+    sums with FP32 drift and E_L (the mixed form) and the FP64 form beside it.
+    Guides: the Pade-Jastrow fallback, and the pair-network Jastrow trained on
+    Be by VMC + SR (the LiH recipe). Energies are the mean of the per-step
+    ensemble energies after n_eq steps, errors by blocking those per-step
+    energies (blocks of 20 steps)."""
+    import numpy as np
+
+    from mole_gb300 import api
+    from mole_gb300 import system as S
+
+    W, tau, exact = 131072, 0.005, -14.66736
+    out = {"workload": "Be DMC, 131072 walkers, tau 0.005, comb every step", "walkers": W, "tau": tau,
+           "exact_ground_state": exact, "eloc_cutoff_in_weights": 2.0 / np.sqrt(tau)}
+
+    def blocked(e, b=20):
+        nb = len(e) // b
+        m = np.asarray(e[: nb * b]).reshape(nb, b).mean(1)
+        return float(m.mean()), float(m.std(ddof=1) / np.sqrt(nb)) if nb > 1 else float("nan")
+
+    cut = 2.0 / np.sqrt(tau)  # E_L window of the weight factor (Umrigar-Nightingale-Runge)
+
+    def run(system, prec, steps, label):
+        wf = api.WaveFunction(ctx, system)
+        wk = api.Walkers(wf, W, seed=0x5EED + 5)
+        api.Sampler(wf, api.MetropolisDiffuse(0.02), wk, precision=prec).run(100, 0, 1)
+        e_ref = api.Sampler(wf, api.MetropolisDiffuse(0.02), wk, precision=prec).run(0, 20, 10).energy
+        dmc = api.DmcRunner(wf, wk, e_ref, precision=prec, eloc_cutoff=cut)
+        e_eq = dmc.run_block(tau, n_eq)
+        dmc.reference_energy = float(np.mean(e_eq[-50:]))
+        ctx.enable_timing(True)
+        torch_sync()
+        t0 = time.perf_counter()
+        e = dmc.run_block(tau, steps)
+        wall = time.perf_counter() - t0
+        ms, n = ctx.kernel_time(1)
+        ctx.enable_timing(False)
+        E, err = blocked(e)
+        r = {"walker_steps_per_s": W * steps / (ms * 1e-3), "ms_per_step": ms / steps,
+             "wall_ms_per_step": 1e3 * wall / steps, "energy": E, "error": err, "acceptance": dmc.acceptance,
+             "steps": steps, "eq_steps": n_eq, "launches_per_step": 4}
+        wk.close()
+        wf.close()
+        return r
+
+    pade = S.beryllium(cusp=True)
+    out["pade_mixed"] = run(pade, api.PREC_MIXED, n_steps, "pade")
+    out["pade_fp64"] = run(pade, api.PREC_FP64, n_steps // 2, "pade64")
+    m, f = out["pade_mixed"], out["pade_fp64"]
+    out["pade_mixed"]["energy_delta_vs_fp64"] = m["energy"] - f["energy"]
+    out["pade_mixed"]["delta_sigma"] = float(np.hypot(m["error"], f["error"]))
+    # neural guide: pair networks trained on Be by VMC + SR from Gaussian(0, 0.01^2) weights
+    s = S.beryllium(neural=True, rng=np.random.default_rng(5))
+    wf = api.WaveFunction(ctx, s)
+    wk = api.Walkers(wf, 16384, seed=0x5EED + 6)
+    samp = api.Sampler(wf, api.MetropolisGaussian(0.3), wk, precision=api.PREC_MIXED)
+    samp.run(300, 0, 1)
+    t0 = time.perf_counter()
+    _, en, er, _ = api.VmcRunner(samp, api.StochasticReconfiguration(0.05, 1e-3, samples=4, sample_every=10,
+                                                                       precision=api.PREC_MIXED)).run_optimization(
+        train_iters, 120, 20)
+    train_s = time.perf_counter() - t0
+    trained = s.with_params(wf.parameters())
+    wk.close()
+    wf.close()
+    out["neural_mixed"] = run(trained, api.PREC_MIXED, n_steps, "neural")
+    out["neural_mixed"].update({"train_iters": train_iters, "train_s": train_s, "vmc_energy_trained": float(en[-1])})
+    return out
+
+
 def torch_sync():
     import torch
 
@@ -539,6 +612,9 @@ def main():
 
             systems, Wb, widths = __import__("mole_gb300.api", fromlist=["api"]).ragged_batch(256)
             line["ragged_batch"]["cpu_baseline"] = cpu_batch_sample(systems, Wb, widths, O.hardware_threads())
+        # -------------------------------------------------- DMC on Be
+        if rank == 0 and world == 1:
+            line["dmc"] = dmc_leg(ctx)
         # -------------------------------------------------- CPU baseline
         if rank == 0 and world == 1:
             from oracle import oracle as O

@@ -132,6 +132,10 @@ typedef struct {
   int32_t n_steps;     /* DMC steps, each a sweep + weight update + comb */
   int32_t precision;   /* MOLE_PREC_* */
   int32_t refresh;     /* steps between FP64 inverse refreshes (0 = 100) */
+  double eloc_cutoff;  /* 0: the raw E_L in the weight, as DmcRunner::diffuse (src/dmc/src/dmc.rs:126-128);
+                          > 0: E_L clipped to e_ref +- eloc_cutoff in the weight factor only (the
+                          Umrigar-Nightingale-Runge 1993 remedy for trial functions that violate
+                          the cusp conditions); the energy estimator keeps the raw E_L */
 } mole_dmc_opts;
 
 /* ---------------------------------------------------------------- context */

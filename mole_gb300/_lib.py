@@ -52,7 +52,7 @@ class VmcOpts(C.Structure):
 
 class DmcOpts(C.Structure):
     _fields_ = [("tau", C.c_double), ("e_ref", C.c_double), ("n_steps", C.c_int32), ("precision", C.c_int32),
-                ("refresh", C.c_int32)]
+                ("refresh", C.c_int32), ("eloc_cutoff", C.c_double)]
 
 
 _P = C.c_void_p

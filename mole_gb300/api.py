@@ -508,16 +508,19 @@ class DmcRunner:
     comb in place of SRBrancher (constant population, equal weights)."""
 
     def __init__(self, guiding_wave_function: WaveFunction, walkers: Walkers, reference_energy: float,
-                 precision: int = PREC_FP64):
+                 precision: int = PREC_FP64, eloc_cutoff: float = 0.0):
         self.wf, self.walkers = guiding_wave_function, walkers
         self.reference_energy = reference_energy
         self.precision = precision
+        # 0: the raw E_L in the weights (the reference's DMC); > 0: clipped to
+        # reference_energy +- eloc_cutoff in the weight factor only
+        self.eloc_cutoff = eloc_cutoff
         self.accepted = 0.0
         self.proposed = 0.0
         self.step_energies: list[np.ndarray] = []
 
     def run_block(self, time_step: float, n_steps: int) -> np.ndarray:
-        o = _lib.DmcOpts(time_step, self.reference_energy, n_steps, self.precision, 0)
+        o = _lib.DmcOpts(time_step, self.reference_energy, n_steps, self.precision, 0, self.eloc_cutoff)
         e = np.zeros(n_steps)
         acc = np.zeros(2)
         check(self.wf.lib.mole_dmc_run(self.walkers.h, C.byref(o), dptr(e), dptr(acc)))

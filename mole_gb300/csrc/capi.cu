@@ -1070,6 +1070,7 @@ int mole_dmc_run(mole_walkers* w, const mole_dmc_opts* o, double* energies, doub
   a.W = W;
   a.tau = o->tau;
   a.e_ref = w->e_ref;
+  a.eloc_cut = o->eloc_cutoff;
   a.seed = w->seed;
   a.step = w->dstep;
   a.partials = c->partials.p;

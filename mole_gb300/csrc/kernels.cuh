@@ -186,6 +186,7 @@ struct DmcArgs {
   int W;
   double tau;
   const double* e_ref; // device scalar
+  double eloc_cut;     // > 0: E_L clipped to e_ref +- eloc_cut in the weight factor
   uint64_t seed;
   const uint64_t* step;  // device step counter
   double* partials;    // [gridDim.x][3]: sum E_old, accepted, proposed
@@ -212,7 +213,13 @@ __global__ void __launch_bounds__(kBlock, (min_blocks<NU, ND>())) dmc_step_kerne
     const double e_new = wk.local_energy(sp, O, nullptr, nullptr);
     wk.store(a.pos, a.W, w);
     a.eloc[w] = e_new;
-    a.weight[w] = exp(-a.tau * (0.5 * (e_old + e_new) - *a.e_ref));
+    const double er = *a.e_ref;
+    double eo = e_old, en = e_new;
+    if (a.eloc_cut > 0.0) {
+      eo = fmin(fmax(eo, er - a.eloc_cut), er + a.eloc_cut);
+      en = fmin(fmax(en, er - a.eloc_cut), er + a.eloc_cut);
+    }
+    a.weight[w] = exp(-a.tau * (0.5 * (eo + en) - er));
     if (!ok) atomicOr(a.status, 2);
     if (!(e_new == e_new)) atomicOr(a.status, 1);
     v[0] = e_old;

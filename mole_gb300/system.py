@@ -250,12 +250,17 @@ def lih(neural: bool = True, rng: np.random.Generator | None = None, b: float = 
                   ee_b=b, nn_on=neural, nn_weights=nn_init(rng) if neural else None, name="LiH")
 
 
-def beryllium(neural: bool = False, rng: np.random.Generator | None = None, b: float = 1.0) -> System:
+def beryllium(neural: bool = False, rng: np.random.Generator | None = None, b: float = 1.0,
+              cusp: bool = False) -> System:
     """Be (Z=4), 2 up / 2 down, 1s/2s STO determinant with a Pade e-e Jastrow
-    and optionally the pairwise-MLP Jastrow."""
+    and optionally the pairwise-MLP Jastrow. With ``cusp`` a Pade e-n term
+    A r / (1 + a r), A = -(Z - zeta_1s), restores the nuclear cusp the 1s
+    exponent alone misses (the DMC guide's Pade fallback)."""
     rng = rng or np.random.default_rng(0x5EED + 5)
     coef = np.eye(2)
+    z1s = 3.7
     return System(nuc_pos=[[0, 0, 0]], nuc_z=[4], n_up=2, n_dn=2, basis_center=[0, 0],
-                  basis_kind=[STO_1S, STO_2S], basis_exp=[0, 1], exponents=[3.7, 0.975], coef_up=coef,
-                  coef_dn=coef, ee_on=True, ee_b=b, nn_on=neural,
+                  basis_kind=[STO_1S, STO_2S], basis_exp=[0, 1], exponents=[z1s, 0.975], coef_up=coef,
+                  coef_dn=coef, ee_on=True, ee_b=b, en_on=cusp, en_a=1.0 if cusp else 0.0,
+                  en_coef=[-(4.0 - z1s)] if cusp else None, nn_on=neural,
                   nn_weights=nn_init(rng) if neural else None, name="Be")

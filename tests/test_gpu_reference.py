@@ -101,3 +101,21 @@ def test_dmc_projects_to_exact_ground_state(ctx, name, system, tau, exact, tol):
     energies, errors = dmc.diffuse(tau, 6000, 200, 5)
     assert abs(energies[-1] - exact) < tol, (energies[-1], errors[-1])
     assert 0.9 < dmc.acceptance <= 1.0
+
+
+def test_be_dmc_with_cusp_guide_and_weight_cutoff_is_stable(ctx):
+    """Be DMC with the Pade guide: the e-n term restores the nuclear cusp and
+    E_L is clipped to E_ref +- 2/sqrt(tau) in the weight factor only; the
+    population energy settles near Be's fixed-node energy instead of
+    running away to the walkers that sit on the nucleus."""
+    s = S.beryllium(cusp=True)
+    wf = api.WaveFunction(ctx, s)
+    wk = api.Walkers(wf, 8192, seed=31)
+    api.Sampler(wf, api.MetropolisDiffuse(0.02), wk).run(100, 0, 1)
+    tau = 0.005
+    dmc = api.DmcRunner(wf, wk, -14.6, precision=api.PREC_MIXED, eloc_cutoff=2.0 / np.sqrt(tau))
+    dmc.run_block(tau, 400)
+    e = dmc.run_block(tau, 400)
+    assert np.all(np.isfinite(e))
+    assert -14.70 < float(np.mean(e)) < -14.62
+    assert 0.95 < dmc.acceptance <= 1.0
