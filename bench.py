@@ -195,10 +195,12 @@ def lih_time_to_sigma(ctx, W: int, train_iters: int, target: float = 1e-3) -> di
         torch.cuda.synchronize()
         mom = np.zeros(7)
         sweeps = 0
+        series = []
         t0 = time.perf_counter()
         while True:
             r = samp.run(0, 20, 10)
             mom += r.moments
+            series.append(r.time_blocks / (W * 10))
             sweeps += 20
             err = api.blocking_error(mom)
             if err <= target or sweeps >= 20000:
@@ -206,7 +208,10 @@ def lih_time_to_sigma(ctx, W: int, train_iters: int, target: float = 1e-3) -> di
         torch.cuda.synchronize()
         secs = time.perf_counter() - t0
         E = mom[1] / mom[0]
+        from mole_gb300 import statistics
+
         leg = {"time_to_sigma_s": secs, "sweeps": sweeps, "energy": E, "error": err,
+               "series_analysis": statistics.analyse(np.concatenate(series)),
                "variance": mom[2] / mom[0] - E * E, "walker_steps_per_s": W * sweeps / secs,
                "train_s": train_s, "train_iters": train_iters, "vmc_kernel_ms_per_launch": v_ms / max(v_n, 1)}
         if neural:

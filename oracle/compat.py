@@ -106,3 +106,39 @@ def comb(weights, u: float) -> np.ndarray:
     c = np.cumsum(w)
     t = (np.arange(w.size) + u) * (c[-1] / w.size)
     return np.minimum(np.searchsorted(c, t, side="right"), w.size - 1)
+
+
+def statfor_correlation(data, max_steps: int = 200):
+    """scripts/statfor.rs:30-54: tau = 1 + 2 sum_i rho(i), i = 1..min(200, n-1),
+    the sum switched off for good at the first negative rho; tau >= 1;
+    returns (tau, n / tau, sqrt(var tau / n)) with var of ddof 1 (statfor.rs:23-26)."""
+    x = np.asarray(data, dtype=np.float64)
+    n = x.size
+    mean = x.mean()
+    var = np.sum((mean - x) ** 2) / (n - 1)
+    tau, f = 1.0, 1.0
+    for i in range(1, min(max_steps, n - 1) + 1):
+        corr = np.sum((x[: n - i] - mean) * (x[i:] - mean)) / (var * (n - i))
+        if corr < 0.0:
+            f = 0.0
+        tau += 2.0 * corr * f
+    tau = max(tau, 1.0)
+    return tau, n / tau, float(np.sqrt(var * tau / n))
+
+
+def statfor_blocking(data, min_left: int = 20, n_sizes: int = 100):
+    """scripts/statfor.rs:57-81: for block sizes 1..n/20 (step max(1, (n/20)/100))
+    the error sqrt((<B^2> - <B>^2) / (n / size - 1)) over data.chunks(size),
+    the last chunk possibly partial. Returns [(size, error)]."""
+    x = np.asarray(data, dtype=np.float64)
+    n = x.size
+    large = n // min_left
+    step = max(large // n_sizes, 1)
+    out = []
+    for size in range(1, large + 1, step):
+        nblocks = n // size
+        means = np.array([c.mean() for c in np.array_split(x, range(size, n, size))])
+        ave_sq = np.mean(means ** 2)
+        ave = np.mean(means)
+        out.append((size, float(np.sqrt((ave_sq - ave * ave) / (nblocks - 1)))))
+    return out
