@@ -379,8 +379,10 @@ def dmc_leg(ctx, n_eq: int = 600, n_steps: int = 800, train_iters: int = 20) -> 
     def run(system, prec, steps, label):
         wf = api.WaveFunction(ctx, system)
         wk = api.Walkers(wf, W, seed=0x5EED + 5)
-        api.Sampler(wf, api.MetropolisDiffuse(0.02), wk, precision=prec).run(100, 0, 1)
-        e_ref = api.Sampler(wf, api.MetropolisDiffuse(0.02), wk, precision=prec).run(0, 20, 10).energy
+        # VMC equilibration with Gaussian moves: the reference's drift-diffusion
+        # acceptance accepts any proposal next to a node (see DmcRunner)
+        api.Sampler(wf, api.MetropolisGaussian(0.3), wk, precision=prec).run(200, 0, 1)
+        e_ref = api.Sampler(wf, api.MetropolisGaussian(0.3), wk, precision=prec).run(0, 20, 10).energy
         dmc = api.DmcRunner(wf, wk, e_ref, precision=prec, eloc_cutoff=cut)
         e_eq = dmc.run_block(tau, n_eq)
         dmc.reference_energy = float(np.mean(e_eq[-50:]))

@@ -314,6 +314,12 @@ int mole_batch_graph_launches(const mole_batch* b, int64_t* n);
  * equal weights. energies[n_steps] receives the per-step ensemble energy
  * sum_w w E_L(old) / sum_w w (dmc.rs:112-135); accept[2] = accepted, proposed. */
 int mole_dmc_run(mole_walkers* w, const mole_dmc_opts* opts, double* energies, double* accept);
+/* Walkers a DMC step found on a node of the guide (an exactly singular Slater
+ * matrix at the precision of its orbital values, psi = 0 there) and gave zero
+ * weight, so the comb removed them; summed over every mole_dmc_run call of
+ * the walker set. The reference has no counterpart (its DMC would divide by
+ * psi = 0). */
+int mole_dmc_node_kills(const mole_walkers* w, double* killed);
 
 /* ------------------------------------------------------------- checkpoints */
 /* Versioned binary dump of positions, step counter, seed and parameters. */

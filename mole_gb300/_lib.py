@@ -94,6 +94,7 @@ SIGNATURES = {
     "mole_sr_collect_solve": (C.c_int, [_P, C.c_double, C.c_double, C.c_int32, C.c_double, _D, _D, _D]),
     "mole_sr_collect_matrix": (C.c_int, [_P, C.c_double, _D]),
     "mole_dmc_run": (C.c_int, [_P, C.POINTER(DmcOpts), _D, _D]),
+    "mole_dmc_node_kills": (C.c_int, [_P, _D]),
     "mole_batch_create": (C.c_int, [_P, C.c_int32, C.POINTER(_P), C.POINTER(C.c_int32), C.POINTER(C.c_uint64), _D,
                                     C.POINTER(_P)]),
     "mole_batch_destroy": (C.c_int, [_P]),

@@ -299,6 +299,15 @@ class MonteCarloResult:
         return 2.0 * (self.sum_EO / n - self.energy * self.sum_O / n)
 
 
+@dataclass
+class ObservableResult:
+    """Per-observable means over walkers and samples, with the blocking error
+    of the per-sample ensemble means (src/vmc/src/vmc.rs:133-172)."""
+    mean: dict
+    error: dict
+    samples: int
+
+
 class Sampler:
     """Sampler (src/montecarlo/src/samplers.rs): a wavefunction, a move and an ensemble."""
 
@@ -326,6 +335,36 @@ class Sampler:
         var = mom[2] / n - E * E if n else float("nan")
         return MonteCarloResult(E, blocking_error(mom), var, mom[5] / max(mom[6], 1.0), mom, tb[: n_steps // block_size],
                                 sO, sEO, sOO)
+
+    def sample_observables(self, observables: dict, n_samples: int, every: int = 1,
+                           block_size: int = 1) -> ObservableResult:
+        """Sampler::sample with user observables (src/montecarlo/src/samplers.rs:81-104):
+        every `every` sweeps the walkers' positions and log-form evaluation are
+        handed to each LocalOperator (mole_gb300.operators) and its walker mean
+        recorded; returns the means over samples and their blocking errors
+        (blocks of `block_size` samples)."""
+        from .operators import WalkerBatch
+
+        wk = self.walkers
+        want_O = any(getattr(o, "needs_O", False) for o in observables.values())
+        series = {k: [] for k in observables}
+        for _ in range(n_samples):
+            self.run(every, 0, 1)
+            ev = wk.evaluate(self.precision, want_O=want_O)
+            b = WalkerBatch(wk.positions(), ev["lnpsi"], ev["sign"], ev["grad"], ev["lap"], ev["eloc"], ev["O"])
+            for k, op in observables.items():
+                series[k].append(np.mean(np.asarray(op.act_on(b), dtype=np.float64), axis=0))
+        mean, err = {}, {}
+        for k, v in series.items():
+            x = np.array(v)
+            mean[k] = x.mean(axis=0)
+            nb = len(x) // block_size
+            if nb > 1:
+                bm = x[: nb * block_size].reshape((nb, block_size) + x.shape[1:]).mean(axis=1)
+                err[k] = np.sqrt(np.maximum((bm * bm).mean(axis=0) - bm.mean(axis=0) ** 2, 0.0) / (nb - 1))
+            else:
+                err[k] = np.full(np.shape(mean[k]), np.nan)
+        return ObservableResult(mean, err, n_samples)
 
 
 class Runner:
@@ -505,7 +544,16 @@ class VmcRunner:
 class DmcRunner:
     """DmcRunner (src/dmc/src/dmc.rs:16-202): drift-diffusion with Metropolis,
     weights exp(-tau((E_L + E_L')/2 - E_ref)) and, every step, a stochastic
-    comb in place of SRBrancher (constant population, equal weights)."""
+    comb in place of SRBrancher (constant population, equal weights).
+
+    The move is the reference's MetropolisDiffuse (src/metropolis/src/metrop.rs:150-198),
+    whose Green's-function ratio includes the drift of every electron: next to
+    a node the unmoved partner's drift (~1/distance) drives the reverse factor
+    to zero and any proposal is accepted, so a walker can be thrown far out. A
+    walker whose Slater matrix is singular at its orbitals' precision (on a
+    node, or with every orbital of an electron underflowed) gets zero weight,
+    is left out of that step's energy and is removed by the comb; node_kills
+    counts them."""
 
     def __init__(self, guiding_wave_function: WaveFunction, walkers: Walkers, reference_energy: float,
                  precision: int = PREC_FP64, eloc_cutoff: float = 0.0):
@@ -553,6 +601,14 @@ class DmcRunner:
     @property
     def acceptance(self) -> float:
         return self.accepted / max(self.proposed, 1.0)
+
+    @property
+    def node_kills(self) -> float:
+        """Walkers found on a node of the guide (psi = 0 at the orbitals'
+        precision) and given zero weight, over this walker set's DMC steps."""
+        k = C.c_double()
+        check(self.wf.lib.mole_dmc_node_kills(self.walkers.h, C.byref(k)))
+        return k.value
 
 
 # ------------------------------------------------------------------ batches

@@ -1041,7 +1041,7 @@ int mole_dmc_run(mole_walkers* w, const mole_dmc_opts* o, double* energies, doub
   const int nb = (W + kScanBlock - 1) / kScanBlock;
   int rc = ensure_dmc(w, o->n_steps);
   if (rc) return rc;
-  CUDA_TRY(c->partials.reserve((size_t)grid * 3));
+  CUDA_TRY(c->partials.reserve((size_t)grid * kDmcPart));
   CUDA_TRY(cudaMemsetAsync(c->status.p, 0, sizeof(int), c->stream));
   if (!w->eloc_valid) {
     // E_L at the current positions seeds E_L(old) of the first step
@@ -1059,10 +1059,13 @@ int mole_dmc_run(mole_walkers* w, const mole_dmc_opts* o, double* energies, doub
     a.status = c->status.p;
     if (mixed) CUDA_TRY(eval32(s)(s->sp32, a, grid, c->stream));
     else CUDA_TRY(eval64(s)(s->sp64, a, grid, c->stream));
+    // walkers this evaluation finds singular are given zero weight by the
+    // first step (which also flags a non-finite E_L of any other walker)
+    CUDA_TRY(cudaMemsetAsync(c->status.p, 0, sizeof(int), c->stream));
     w->eloc_valid = true;
   }
   const uint64_t step = w->step;
-  CombState cs0 = {0.0, 0.0, 0.0, 0.0};
+  CombState cs0 = {0.0, 0.0, 0.0, 0.0, 0.0};
   CUDA_TRY(cudaMemcpyAsync(w->dstep, &step, sizeof(uint64_t), cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(cudaMemcpyAsync(w->e_ref, &o->e_ref, sizeof(double), cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(cudaMemcpyAsync(w->comb, &cs0, sizeof(CombState), cudaMemcpyHostToDevice, c->stream));
@@ -1094,11 +1097,18 @@ int mole_dmc_run(mole_walkers* w, const mole_dmc_opts* o, double* energies, doub
   CUDA_TRY(cudaMemcpyAsync(&cs, w->comb, sizeof(CombState), cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(cudaStreamSynchronize(c->stream));
   w->step += (uint64_t)o->n_steps;
+  w->dmc_node_kills += cs.killed;
   if (accept) {
     accept[0] = cs.accepted;
     accept[1] = cs.proposed;
   }
   return check_status(c);
+}
+
+int mole_dmc_node_kills(const mole_walkers* w, double* killed) {
+  if (!w || !killed) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
+  *killed = w->dmc_node_kills;
+  return MOLE_OK;
 }
 
 // checkpoint: "MOLECKP1", W, N, P, seed, step, theta[P], positions [W][N][3]

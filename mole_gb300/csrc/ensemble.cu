@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(kScanBlock) scan_blocks_kernel(const double* w
 // step counter increment.
 __global__ void scan_totals_kernel(double* btot, int nb, const double* partials, int n_part, CombState* cs,
                                    uint64_t* step, uint64_t seed, double* energies, int64_t e_index, int W) {
-  __shared__ double sh[3];
+  __shared__ double sh[4];
   if (threadIdx.x == 0) {
     double run = 0.0;
     for (int b = 0; b < nb; ++b) {
@@ -112,16 +112,17 @@ __global__ void scan_totals_kernel(double* btot, int nb, const double* partials,
     const uint4 u = draw4(seed, 0u, (uint32_t)(*step), 0u, kTagComb);
     cs->u = u01<double>(u.x);
   }
-  if (threadIdx.x < 3) {
+  if (threadIdx.x < 4) {  // partials rows: sum E_old, accepted, proposed, walkers on a node
     double s = 0.0;
-    for (int r = 0; r < n_part; ++r) s += partials[(size_t)r * 3 + threadIdx.x];
+    for (int r = 0; r < n_part; ++r) s += partials[(size_t)r * 4 + threadIdx.x];
     sh[threadIdx.x] = s;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    energies[e_index] = sh[0] / W;
+    energies[e_index] = sh[0] / ((double)W - sh[3]);  // over the walkers with weight
     cs->accepted += sh[1];
     cs->proposed += sh[2];
+    cs->killed += sh[3];
     *step += 1;
   }
 }

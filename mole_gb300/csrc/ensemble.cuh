@@ -12,6 +12,7 @@ struct CombState {
   double u;         // the comb's one uniform
   double accepted;  // running accepted moves
   double proposed;  // running proposed moves
+  double killed;    // running count of walkers given zero weight on a node of the guide
 };
 
 cudaError_t launch_init_positions(double* pos, int W, int N, uint64_t seed, int kind, double width, cudaStream_t s);

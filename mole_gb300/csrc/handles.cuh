@@ -95,6 +95,7 @@ struct mole_walkers {
   uint64_t* dstep = nullptr;
   CombState* comb = nullptr;
   bool eloc_valid = false;
+  double dmc_node_kills = 0.0;  // walkers given zero weight on a node of the guide, all DMC calls
   // many-parameter SR (allocated on first use)
   SrLargeState* srl = nullptr;
   CUtensorMap* srl_map = nullptr;

@@ -189,47 +189,56 @@ struct DmcArgs {
   double eloc_cut;     // > 0: E_L clipped to e_ref +- eloc_cut in the weight factor
   uint64_t seed;
   const uint64_t* step;  // device step counter
-  double* partials;    // [gridDim.x][3]: sum E_old, accepted, proposed
+  double* partials;    // [gridDim.x][kDmcPart]: sum E_old, accepted, proposed, walkers on a node
   int* status;
 };
+constexpr int kDmcPart = 4;
 
 template <int NU, int ND, class R, bool EN, bool NN = false>
 __global__ void __launch_bounds__(kBlock, (min_blocks<NU, ND>())) dmc_step_kernel(const __grid_constant__ SysParams<R> sp, const DmcArgs a) {
   using Wk = Walker<NU, ND, R, 0, EN, NN>;
-  __shared__ double red[3 * kBlock / 32];
+  __shared__ double red[kDmcPart * kBlock / 32];
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = w < a.W;
   const uint32_t t = (uint32_t)(*a.step);
-  double v[3] = {0.0, 0.0, 0.0};
+  double v[kDmcPart] = {0.0, 0.0, 0.0, 0.0};
   const NnCtx<R> nnc = nn_setup<R, NN>(sp);
   if (active) {
     Wk wk;
     wk.nn = nnc;
     wk.load(a.pos, a.W, w);
-    bool ok = wk.refresh(sp, nullptr, nullptr);
     const double e_old = a.eloc[w];
-    const int nacc = wk.template sweep<kMoveDiffuse>(sp, (R)a.tau, a.seed, (uint32_t)w, t);
-    double O[1];
-    const double e_new = wk.local_energy(sp, O, nullptr, nullptr);
-    wk.store(a.pos, a.W, w);
-    a.eloc[w] = e_new;
-    const double er = *a.e_ref;
-    double eo = e_old, en = e_new;
-    if (a.eloc_cut > 0.0) {
-      eo = fmin(fmax(eo, er - a.eloc_cut), er + a.eloc_cut);
-      en = fmin(fmax(en, er - a.eloc_cut), er + a.eloc_cut);
-    }
-    a.weight[w] = exp(-a.tau * (0.5 * (eo + en) - er));
-    if (!ok) atomicOr(a.status, 2);
-    if (!(e_new == e_new)) atomicOr(a.status, 1);
-    v[0] = e_old;
-    v[1] = (double)nacc;
     v[2] = (double)Wk::N;
+    if (!wk.refresh(sp, nullptr, nullptr)) {
+      // an exactly singular Slater matrix: psi = 0 at the precision of the
+      // orbital values (the walker sits on a node, or an electron is so far
+      // out that every orbital underflows), so the walker carries no weight,
+      // is left out of this step's energy and is removed by the comb
+      a.weight[w] = 0.0;
+      v[3] = 1.0;
+    } else {
+      v[0] = e_old;
+      if (!(e_old == e_old)) atomicOr(a.status, 1);
+      const int nacc = wk.template sweep<kMoveDiffuse>(sp, (R)a.tau, a.seed, (uint32_t)w, t);
+      double O[1];
+      const double e_new = wk.local_energy(sp, O, nullptr, nullptr);
+      wk.store(a.pos, a.W, w);
+      a.eloc[w] = e_new;
+      const double er = *a.e_ref;
+      double eo = e_old, en = e_new;
+      if (a.eloc_cut > 0.0) {
+        eo = fmin(fmax(eo, er - a.eloc_cut), er + a.eloc_cut);
+        en = fmin(fmax(en, er - a.eloc_cut), er + a.eloc_cut);
+      }
+      a.weight[w] = exp(-a.tau * (0.5 * (eo + en) - er));
+      if (!(e_new == e_new)) atomicOr(a.status, 1);
+      v[1] = (double)nacc;
+    }
   }
-  block_sum<3>(v, red);
+  block_sum<kDmcPart>(v, red);
   if (threadIdx.x == 0)
 #pragma unroll
-    for (int k = 0; k < 3; ++k) a.partials[(size_t)blockIdx.x * 3 + k] = v[k];
+    for (int k = 0; k < kDmcPart; ++k) a.partials[(size_t)blockIdx.x * kDmcPart + k] = v[k];
 }
 
 }  // namespace mole

@@ -287,14 +287,37 @@ __global__ void __launch_bounds__(128, 1) s_gemm_kernel(const __grid_constant__ 
   uint32_t* tmem_slot = (uint32_t*)(done + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-  // upper-triangular tile (ti <= tj) of this CTA
+  // upper-triangular tile (ti <= tj) of this CTA, in bands of kSBand tile
+  // rows walked column by column: CTAs running together share B panels, and
+  // a band's A panels stay in L2 while its columns stream past
   const int T = P_pad / kSBM;
-  int ti = 0, rem = blockIdx.x;
-  while (rem >= T - ti) {
-    rem -= T - ti;
-    ++ti;
+  int ti = 0, tj = 0;
+  {
+    int rem = blockIdx.x;
+    for (int r0 = 0; r0 < T; r0 += kSBand) {
+      const int r1 = min(r0 + kSBand, T);
+      const int tri = (r1 - r0) * (r1 - r0 + 1) / 2;  // columns r0..r1-1 (diagonal part)
+      const int band = tri + (T - r1) * (r1 - r0);
+      if (rem >= band) {
+        rem -= band;
+        continue;
+      }
+      if (rem < tri) {
+        int c = 0;
+        while (rem >= c + 1) {
+          rem -= c + 1;
+          ++c;
+        }
+        tj = r0 + c;
+        ti = r0 + rem;
+      } else {
+        rem -= tri;
+        tj = r1 + rem / (r1 - r0);
+        ti = r0 + rem % (r1 - r0);
+      }
+      break;
+    }
   }
-  const int tj = ti + rem;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kSStages; ++s) {
@@ -342,14 +365,19 @@ __global__ void __launch_bounds__(128, 1) s_gemm_kernel(const __grid_constant__ 
     umma_commit(done);
   }
   __syncwarp();
-  // epilogue: every thread owns one row of the 128 x 128 tile
+  // epilogue: thread (warp, lane) reads row 32 warp + lane of the tile from
+  // TMEM, 16 columns at a time, into a shared staging tile (the pipeline's
+  // buffers, idle once `done` has fired); the warp then adds its 32 rows to
+  // S two rows per instruction, 16 consecutive doubles per half-warp
   const bool got = mbar_wait(done, 0);
   if (!ok || !got) {
     if (lane == 0) atomicOr(status, 4);
   } else {
     asm volatile("tcgen05.fence::after_thread_sync;");
+    constexpr int LD = 17;  // staging row stride (doubles), odd: conflict-free columns
+    double* stage = reinterpret_cast<double*>(tiles) + (size_t)warp * 32 * LD;
     const int row = warp * 32 + lane;
-    double* out = S + (size_t)(ti * kSBM + row) * P_pad + tj * kSBM;
+    const int half = lane >> 4, col = lane & 15;
 #pragma unroll 1
     for (int c0 = 0; c0 < kSBM; c0 += 16) {
       uint32_t v[16];
@@ -362,8 +390,18 @@ __global__ void __launch_bounds__(128, 1) s_gemm_kernel(const __grid_constant__ 
           : "r"(taddr));
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-      for (int i = 0; i < 16; ++i) out[c0 + i] += (double)__uint_as_float(v[i]);
+      for (int i = 0; i < 16; ++i) stage[lane * LD + i] = (double)__uint_as_float(v[i]);
+      __syncwarp();
+      // all 16 loads of the chunk in flight before the first store
+      double* out0 = S + (size_t)(ti * kSBM + warp * 32 + half) * P_pad + tj * kSBM + c0 + col;
+      double old[16];
+#pragma unroll
+      for (int k = 0; k < 16; ++k) old[k] = out0[(size_t)(2 * k) * P_pad];
+#pragma unroll
+      for (int k = 0; k < 16; ++k) out0[(size_t)(2 * k) * P_pad] = old[k] + stage[(2 * k + half) * LD + col];
+      __syncwarp();
     }
+    (void)row;
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();

@@ -14,6 +14,7 @@ namespace mole {
 constexpr int kSBM = 128;
 constexpr int kSBK = 64;
 constexpr int kSStages = 4;
+constexpr int kSBand = 16;  // tile rows per band of the tile order
 constexpr uint32_t kSTileBytes = kSBM * kSBK * 2;  // one BF16 operand tile, 16 KB
 constexpr size_t kSGemmSmem = 2 * kSStages * (size_t)kSTileBytes + 1024 + 256;
 

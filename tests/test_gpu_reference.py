@@ -119,3 +119,5 @@ def test_be_dmc_with_cusp_guide_and_weight_cutoff_is_stable(ctx):
     assert np.all(np.isfinite(e))
     assert -14.70 < float(np.mean(e)) < -14.62
     assert 0.95 < dmc.acceptance <= 1.0
+    # walkers the FP32 orbitals put exactly on the |r1| = |r2| node are rare
+    assert dmc.node_kills < 1e-4 * 8192 * 800
