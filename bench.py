@@ -351,6 +351,45 @@ def ragged_batch_leg(ctx, steps: int, sweeps: int = 100) -> dict:
     return out
 
 
+def helium_leg(ctx) -> dict:
+    """The helium singlet at its full size, the reference's own CPU-runnable
+    case: Z = 2, psi = exp(-alpha (r1 + r2)) exp(r12 / (2 (1 + beta r12))),
+    alpha 1.6875, beta 0.3, 1,024 walkers started N(0, 1) bohr, box moves of
+    side 0.5 bohr, 1,000 unsampled + 10,000 sampled sweeps, E_L every sweep,
+    FP64 (and the mixed form beside it); the CPU port runs the same workload
+    on all host threads."""
+    import numpy as np
+
+    from mole_gb300 import api
+    from mole_gb300 import system as S
+    from oracle import oracle as O
+
+    W, n_eq, n_steps = 1024, 1000, 10000
+    out = {"workload": "He singlet VMC, 1024 walkers, box 0.5 bohr, 1000 + 10000 sweeps", "walkers": W}
+    for name, prec in (("fp64", api.PREC_FP64), ("mixed", api.PREC_MIXED)):
+        wf = api.WaveFunction(ctx, S.helium(1.6875, 0.3))
+        wk = api.Walkers(wf, W, seed=0x5EED)
+        samp = api.Sampler(wf, api.MetropolisBox(0.5), wk, precision=prec)
+        samp.run(10, 0, 1)  # warm-up launch (module load)
+        wk.init()
+        wk.step = 0
+        torch_sync()
+        t0 = time.perf_counter()
+        r = samp.run(n_eq, n_steps, 100)
+        secs = time.perf_counter() - t0
+        out[name] = {"value": W * (n_eq + n_steps) / secs, "unit": "walker-steps/s", "seconds": secs,
+                     "energy": r.energy, "error": r.error, "acceptance": r.acceptance}
+        wk.close()
+        wf.close()
+    threads = O.hardware_threads()
+    O.build()
+    secs, e = O.faithful_vmc(0, W, n_eq, n_steps, 0, 0.5, 1.6875, 0.3, False, threads, 1)
+    out["cpu_baseline"] = {"value": W * (n_eq + n_steps) / secs, "unit": "walker-steps/s", "cores": threads,
+                           "kind": "port", "energy": e, "sample": f"the whole workload ({secs:.2f} s), reference call "
+                                                                  "pattern (oracle/faithful.cpp)"}
+    return out
+
+
 def dmc_leg(ctx, n_eq: int = 600, n_steps: int = 800, train_iters: int = 20) -> dict:
     """DMC on the Be atom (Z = 4, 2 up + 2 down, 1s/2s STO determinant):
     131,072 walkers, time step 0.005, drift-diffusion moves with Metropolis
@@ -619,6 +658,9 @@ def main():
 
             systems, Wb, widths = __import__("mole_gb300.api", fromlist=["api"]).ragged_batch(256)
             line["ragged_batch"]["cpu_baseline"] = cpu_batch_sample(systems, Wb, widths, O.hardware_threads())
+        # -------------------------------------------------- helium, full size
+        if rank == 0 and world == 1:
+            line["helium"] = helium_leg(ctx)
         # -------------------------------------------------- DMC on Be
         if rank == 0 and world == 1:
             line["dmc"] = dmc_leg(ctx)

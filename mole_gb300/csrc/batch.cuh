@@ -252,18 +252,21 @@ __device__ __forceinline__ int batch_move(const SysParams<R>& sp, const BatchWal
   const uint4 ra = draw4(seed, wid, t, 2u * e, kTagMove);
   R dx[3];  // in the FP32 form the move is made on the FP32 copy; FP64 only on acceptance
   R uacc;
+  uint32_t ubits;
   float z[3];
   if constexpr (MOVE == kMoveBox) {
     dx[0] = step * (u01<R>(ra.x) - (R)0.5);
     dx[1] = step * (u01<R>(ra.y) - (R)0.5);
     dx[2] = step * (u01<R>(ra.z) - (R)0.5);
     uacc = u01<R>(ra.w);
+    ubits = ra.w;
   } else {
     float z3;
     repro_box_muller(ra.x, ra.y, z[0], z[1]);
     repro_box_muller(ra.z, ra.w, z[2], z3);
     const uint4 rb = draw4(seed, wid, t, 2u * e + 1u, kTagMove);
     uacc = u01<R>(rb.x);
+    ubits = rb.x;
 #pragma unroll
     for (int c = 0; c < 3; ++c) dx[c] = step * (R)z[c];
   }
@@ -299,8 +302,7 @@ __device__ __forceinline__ int batch_move(const SysParams<R>& sp, const BatchWal
           batch_pair_u<R>(sp, same, ro[0] - xj[0], ro[1] - xj[1], ro[2] - xj[2]);
   }
   if constexpr (F64) {
-    const double p = ratio * ratio * exp(2.0 * dJ);
-    if (!(p > uacc)) return 0;
+    if (!metropolis_accept(ratio, 2.0 * dJ, ubits)) return 0;
   } else {
     const float rf = (float)ratio;  // the acceptance test itself is a random comparison: FP32
     if (!(rf * rf * __expf(2.0f * dJ) > uacc)) return 0;

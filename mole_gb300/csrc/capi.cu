@@ -647,7 +647,8 @@ int mole_vmc_run(mole_walkers* w, const mole_vmc_opts* o, double* moments, doubl
   auto f64 = vmc64(s, slot, drift);
   auto f32 = vmc32(s, slot, drift);
   if (mixed ? !f32 : !f64) return fail(MOLE_ERR_UNSUPPORTED, "SR kernel not compiled for this family and precision");
-  const int W = w->W, grid = grid_for(W), NA = n_acc(PM);
+  int wpc = kBlock;
+  const int W = w->W, grid = vmc_grid(W, s->n_up, s->n_dn, c->n_sm, &wpc), NA = n_acc(PM);
   const int n_tb = o->n_steps / o->block_size;
   CUDA_TRY(c->partials.reserve((size_t)grid * NA));
   CUDA_TRY(c->tb_partials.reserve((size_t)grid * std::max(n_tb, 1)));
@@ -664,6 +665,7 @@ int mole_vmc_run(mole_walkers* w, const mole_vmc_opts* o, double* moments, doubl
   a.refresh = o->refresh;
   a.seed = w->seed;
   a.step0 = (uint32_t)w->step;
+  a.wpc = wpc;
   a.partials = c->partials.p;
   a.tb_partials = c->tb_partials.p;
   a.status = c->status.p;
@@ -752,7 +754,8 @@ int mole_vmc_run_noalloc(const mole_system* s, double* d_pos, int32_t W, uint64_
   auto f64 = vmc64(s, slot, drift);
   auto f32 = vmc32(s, slot, drift);
   if (mixed ? !f32 : !f64) return fail(MOLE_ERR_UNSUPPORTED, "kernel not compiled for this family and precision");
-  const int grid = grid_for(W), NA = n_acc(PM), n_tb = o->n_steps / o->block_size;
+  int wpc = kBlock;
+  const int grid = vmc_grid(W, s->n_up, s->n_dn, s->ctx->n_sm, &wpc), NA = n_acc(PM), n_tb = o->n_steps / o->block_size;
   // scratch layout: partials [grid][NA] | time-block partials [grid][n_tb] | reduced [NA] | status
   const size_t need = (size_t)grid * NA + (size_t)grid * n_tb + NA + 1;
   if (need > kNoAllocScratchDoubles)
@@ -781,6 +784,7 @@ int mole_vmc_run_noalloc(const mole_system* s, double* d_pos, int32_t W, uint64_
   a.refresh = o->refresh;
   a.seed = seed;
   a.step0 = (uint32_t)step0;
+  a.wpc = wpc;
   a.partials = partials;
   a.tb_partials = tb_partials;
   a.status = status;

@@ -13,6 +13,25 @@ template <int NU, int ND>
 constexpr int min_blocks() {
   return (NU + ND) <= 2 ? 7 : ((NU + ND) <= 4 ? 4 : 2);
 }
+__host__ __device__ inline int min_blocks_rt(int nu, int nd) {
+  return (nu + nd) <= 2 ? 7 : ((nu + nd) <= 4 ? 4 : 2);
+}
+
+// VMC grid: with walkers for at least half a wave the grid is a whole number
+// of waves of (SMs x resident CTAs) and the walkers are split evenly over the
+// CTAs (every SM gets the same number of walkers); smaller ensembles use
+// full 64-walker CTAs. Returns the grid and sets *wpc, walkers per CTA.
+inline int vmc_grid(int W, int nu, int nd, int n_sm, int* wpc) {
+  const int g = (W + kBlock - 1) / kBlock;
+  const int cap = n_sm * min_blocks_rt(nu, nd);
+  if (n_sm <= 0 || 2 * g < cap) {
+    *wpc = kBlock;
+    return g;
+  }
+  const int grid = cap * ((g + cap - 1) / cap);
+  *wpc = (W + grid - 1) / grid;
+  return grid;
+}
 
 // Accumulators per walker: moments first, then SR sums.
 constexpr int kNMom = 7;  // count, sumE, sumE2, sumBlock2, nBlocks, accept, proposed
@@ -26,6 +45,7 @@ struct VmcArgs {
   int n_eq, n_steps, block_size, refresh;
   uint64_t seed;
   uint32_t step0;
+  int wpc;              // walkers per CTA (<= blockDim.x): CTA b runs walkers [b wpc, (b + 1) wpc)
   double* partials;     // [gridDim.x][n_acc]
   double* tb_partials;  // [gridDim.x][n_steps / block_size]
   int* status;          // bit 0: non-finite E_L; bit 1: singular determinant
@@ -55,9 +75,9 @@ __device__ __forceinline__ void vmc_body(const SysParams<R>& sp, const VmcArgs& 
   using Wk = Walker<NU, ND, R, PM, EN, NN>;
   constexpr int NA = n_acc(PM);
   constexpr int NSR = NA - kNMom;
-  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  const int w = blockIdx.x * a.wpc + threadIdx.x;
   const int tid = threadIdx.x;
-  const bool active = w < a.W;
+  const bool active = tid < a.wpc && w < a.W;
   Wk wk;
   wk.nn = nn_setup<R, NN>(sp);
   if (active) wk.load(a.pos, a.W, w);

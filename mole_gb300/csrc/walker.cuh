@@ -255,6 +255,25 @@ __device__ __forceinline__ void pair_vals(const SysParams<R>& sp, bool same, R d
   v.l += uRR * Rp * Rp + uR * Rpp + (R)2 * f;
 }
 
+// The Metropolis test ratio^2 exp(x) > u, u = u01(ubits) >= 2^-33. With
+// |x| < 80 and 1e-30 < ratio^2 < 1e30 the FP32 value of ratio^2 exp(x) is
+// within 2e-5 relative of the exact one while it is a normal float, and it
+// under- (over-) flows only when the exact value is below 1e-38 (above
+// 3e38), i.e. far below (above) any u; so where it is clear of u by 1e-3
+// relative it decides exactly as the FP64 test. Everything else takes the
+// FP64 expression. Same decisions as FP64, the FP64 exp skipped in all but
+// borderline and extreme cases.
+__device__ __forceinline__ bool metropolis_accept(double ratio, double x, uint32_t ubits) {
+  const float rf = (float)ratio, xf = (float)x;
+  const float r2 = rf * rf;
+  if (fabsf(xf) < 80.f && r2 > 1e-30f && r2 < 1e30f) {
+    const float uf = u01<float>(ubits);
+    const float d = r2 * __expf(xf) - uf;
+    if (fabsf(d) > 1e-3f * uf) return d > 0.f;
+  }
+  return ratio * ratio * exp(x) > u01<double>(ubits);
+}
+
 // In-register Gauss-Jordan inverse with partial pivoting; row swaps are
 // predicated so that every index stays compile-time.
 template <int n>
@@ -495,17 +514,20 @@ struct Walker {
     const uint4 ra = draw4(seed, wid, t, 2u * e, kTagMove);
     double dx[3];
     R uacc;
+    uint32_t ubits;
     if constexpr (MOVE == kMoveBox) {
       dx[0] = (double)(step * (u01<R>(ra.x) - (R)0.5));
       dx[1] = (double)(step * (u01<R>(ra.y) - (R)0.5));
       dx[2] = (double)(step * (u01<R>(ra.z) - (R)0.5));
       uacc = u01<R>(ra.w);
+      ubits = ra.w;
     } else {
       float z0, z1, z2, z3;
       repro_box_muller(ra.x, ra.y, z0, z1);
       repro_box_muller(ra.z, ra.w, z2, z3);
       const uint4 rb = draw4(seed, wid, t, 2u * e + 1u, kTagMove);
       uacc = u01<R>(rb.x);
+      ubits = rb.x;
       if constexpr (MOVE == kMoveGauss) {
         dx[0] = (double)step * (double)z0;
         dx[1] = (double)step * (double)z1;
@@ -540,8 +562,12 @@ struct Walker {
     bool acc;
     double bn[n * n];
     if constexpr (!DRIFT) {
-      const double p = ratio * ratio * (double)exp_t<R>((R)2 * dJ);
-      acc = p > (double)uacc;
+      if constexpr (std::is_same<R, double>::value) {
+        acc = metropolis_accept(ratio, 2.0 * dJ, ubits);
+      } else {
+        const double p = ratio * ratio * (double)exp_t<R>((R)2 * dJ);
+        acc = p > (double)uacc;
+      }
     } else {
       // tentative inverse after replacing row i
       double v[n];
@@ -609,8 +635,11 @@ struct Walker {
         }
       });
       const double la = 2.0 * (double)dJ - (hi - lo) / (2.0 * (double)step);
-      const double p = ratio * ratio * exp(la);
-      acc = (ratio > 0.0) && (p > (double)uacc);
+      if constexpr (std::is_same<R, double>::value) {
+        acc = (ratio > 0.0) && metropolis_accept(ratio, la, ubits);
+      } else {
+        acc = (ratio > 0.0) && (ratio * ratio * exp(la) > (double)uacc);
+      }
     }
     if (!acc) return 0;
 
