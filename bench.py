@@ -387,6 +387,10 @@ def helium_leg(ctx) -> dict:
     out["cpu_baseline"] = {"value": W * (n_eq + n_steps) / secs, "unit": "walker-steps/s", "cores": threads,
                            "kind": "port", "energy": e, "sample": f"the whole workload ({secs:.2f} s), reference call "
                                                                   "pattern (oracle/faithful.cpp)"}
+    osecs, oe, _ = O.optimized_vmc(0, W, n_eq, n_steps, 0.5, 1.6875, 0.3, threads)
+    out["cpu_optimized"] = {"value": W * (n_eq + n_steps) / osecs, "unit": "walker-steps/s", "cores": threads,
+                            "energy": oe, "sample": f"the whole workload with Gaussian moves ({osecs:.2f} s), "
+                                                    "cached terms (oracle/optimized.cpp)"}
     return out
 
 
@@ -675,6 +679,13 @@ def main():
             line["cpu_baseline"] = {"value": rate, "unit": "walker-steps/s", "cores": threads, "kind": "port",
                                     "sample": f"{wk_cpu} walkers x 2000 sweeps ({secs:.1f} s), reference call "
                                               "pattern (oracle/faithful.cpp), std::thread over all host cores"}
+            # beside it, for an honest ratio: the GPU kernel's algorithm on the CPU
+            osecs, _, _ = O.optimized_vmc(1, 64 * threads, 0, 200, 0.4, 1.0, 0.5, threads)
+            wo = int(max(1, round(12.0 * 64 * threads * 200 / osecs / 2000 / threads / 64))) * 64 * threads
+            osecs, oe, _ = O.optimized_vmc(1, wo, 0, 2000, 0.4, 1.0, 0.5, threads)
+            line["cpu_optimized"] = {"value": wo * 2000 / osecs, "unit": "walker-steps/s", "cores": threads,
+                                     "kind": "port", "sample": f"{wo} walkers x 2000 sweeps ({osecs:.1f} s), "
+                                     "cached orbital and pair terms, no allocation (oracle/optimized.cpp)"}
     if rank == 0:
         print(json.dumps(line, default=_json_default), flush=True)
     if world > 1:

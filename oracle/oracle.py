@@ -231,6 +231,9 @@ def faithful_lib() -> C.CDLL:
         L.faithful_vmc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                    C.c_int, C.c_int, C.c_uint64, C.POINTER(C.c_double)]
         L.faithful_hardware_threads.restype = C.c_int
+        L.optimized_vmc.restype = C.c_double
+        L.optimized_vmc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int,
+                                    C.c_uint64, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L._typed = True
     return L
 
@@ -242,6 +245,16 @@ def faithful_vmc(system: int, n_walkers: int, n_eq: int, n_steps: int, move: int
     t = faithful_lib().faithful_vmc(system, n_walkers, n_eq, n_steps, move, step, a, b, int(sr), threads, seed,
                                     C.byref(e))
     return t, e.value
+
+
+def optimized_vmc(system: int, n_walkers: int, n_eq: int, n_steps: int, step: float, a: float, b: float,
+                  threads: int, seed: int = 1):
+    """Times the optimised CPU port (cached terms, no allocation); returns
+    (seconds, mean energy, acceptance)."""
+    e, acc = C.c_double(), C.c_double()
+    t = faithful_lib().optimized_vmc(system, n_walkers, n_eq, n_steps, step, a, b, threads, seed, C.byref(e),
+                                     C.byref(acc))
+    return t, e.value, acc.value
 
 
 def hardware_threads() -> int:
