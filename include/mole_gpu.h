@@ -221,7 +221,7 @@ int mole_vmc_run(mole_walkers* w, const mole_vmc_opts* opts, double* moments, do
  * the caller advances step0 by n_eq + n_steps itself). The library's only
  * working memory is one fixed 2 MiB device array that every GPU loading the
  * library holds until the process exits; the call is rejected with
- * MOLE_ERR_SHAPE when ceil(W / 64) x (accumulators + time blocks) does not
+ * MOLE_ERR_SHAPE when (CTAs of the launch) x (accumulators + time blocks) does not
  * fit it. The first call on a device looks up that array's device address,
  * so make it before any stream capture. Every call shares the array: calls
  * that overlap on the GPU (other streams, other threads) race. The call
