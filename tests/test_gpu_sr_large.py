@@ -33,7 +33,10 @@ def test_network_log_derivatives_match_oracle(ctx):
     assert np.max(np.abs(g[:, nw:] - r[:, nw:]) / scale) < 2e-4
 
 
-def test_tensor_core_s_matrix_and_cg_solve(ctx):
+@pytest.mark.parametrize("n_samples", [3, 6])
+def test_tensor_core_s_matrix_and_cg_solve(ctx, n_samples):
+    # 3 samples: one GEMM launch over 3 chunks at the solve; 6: a launch over
+    # 4 chunks when Ot fills (storing S), then one over 2 adding to it
     s = lih_nn(std=0.1)
     wf = api.WaveFunction(ctx, s)
     W = 512
@@ -42,7 +45,7 @@ def test_tensor_core_s_matrix_and_cg_solve(ctx):
     samp.run(50, 0, 1)
     Os, Es = [], []
     wk.sr_collect_begin()
-    for _ in range(3):
+    for _ in range(n_samples):
         samp.run(0, 5, 5)
         ev = wk.evaluate(api.PREC_MIXED)
         Os.append(ev["O"])
