@@ -352,6 +352,13 @@ struct Walker {
   double x[N][3];
   double bu[NU * NU];    // inverse of the up Slater matrix, bu[k*NU+i]
   double bd[NDm * NDm];  // inverse of the down Slater matrix
+  // The FP32 form's drift-diffusion move computes drifts and Green's-function
+  // sums in FP32 from an FP32 copy of the inverses (set at every refresh and
+  // every accepted drift move); ratios and updates stay on the FP64 ones.
+  static constexpr bool F32 = std::is_same<R, float>::value;
+  using D = typename std::conditional<F32, float, double>::type;  // drift arithmetic
+  float bfu[F32 ? NU * NU : 1];
+  float bfd[F32 ? NDm * NDm : 1];
   // one-body caches
   R og[N][NMAX][3], ol[N][NMAX];
   R odz[N][NMAX][NZC];
@@ -436,6 +443,12 @@ struct Walker {
     double l1 = 0.0, s1 = 1.0, l2 = 0.0, s2 = 1.0;
     bool ok = gj_invert<NU>(au, bu, lndet ? &l1 : nullptr, &s1);
     if constexpr (ND > 0) ok = gj_invert<ND>(ad, bd, lndet ? &l2 : nullptr, &s2) && ok;
+    if constexpr (F32) {
+#pragma unroll
+      for (int k = 0; k < NU * NU; ++k) bfu[k] = (float)bu[k];
+#pragma unroll
+      for (int k = 0; k < (ND > 0 ? ND * ND : 0); ++k) bfd[k] = (float)bd[k];
+    }
     double J = 0.0;
 #pragma unroll
     for (int e = 0; e < N; ++e) J += (double)jen[e];
@@ -471,6 +484,26 @@ struct Walker {
       g[c] = s;
     }
   }
+  // grad ln det at electron j in the drift arithmetic (FP32 copy of B in the FP32 form)
+  template <int j>
+  __device__ __forceinline__ void det_grad_d(D (&g)[3]) const {
+    if constexpr (F32) {
+      constexpr bool isup = j < NU;
+      constexpr int n = isup ? NU : ND;
+      constexpr int i = isup ? j : j - NU;
+      constexpr int ld = isup ? NU : NDm;
+      const float* B = isup ? bfu : bfd;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        float s = 0.f;
+#pragma unroll
+        for (int k = 0; k < n; ++k) s += og[j][k][c] * B[k * ld + i];
+        g[c] = s;
+      }
+    } else {
+      det_grad<j>(g);
+    }
+  }
   // grad J at electron j from the caches
   template <int j>
   __device__ __forceinline__ void jas_grad(R (&g)[3]) const {
@@ -498,16 +531,16 @@ struct Walker {
     double* B = isup ? bu : bd;
 
     // drift at the current configuration (diffuse moves)
-    double vcur[N][3];
+    D vcur[N][3];
     if constexpr (DRIFT) {
       static_for<0, N>([&](auto jc) {
         constexpr int j = decltype(jc)::value;
-        double gdj[3];
+        D gdj[3];
         R gjj[3];
-        det_grad<j>(gdj);
+        det_grad_d<j>(gdj);
         jas_grad<j>(gjj);
 #pragma unroll
-        for (int c = 0; c < 3; ++c) vcur[j][c] = gdj[c] + (double)gjj[c];
+        for (int c = 0; c < 3; ++c) vcur[j][c] = gdj[c] + (D)gjj[c];
       });
     }
 
@@ -532,6 +565,11 @@ struct Walker {
         dx[0] = (double)step * (double)z0;
         dx[1] = (double)step * (double)z1;
         dx[2] = (double)step * (double)z2;
+      } else if constexpr (F32) {
+        const float sq = sqrtf(step);
+        dx[0] = (double)(step * vcur[e][0] + sq * z0);
+        dx[1] = (double)(step * vcur[e][1] + sq * z1);
+        dx[2] = (double)(step * vcur[e][2] + sq * z2);
       } else {
         const double sq = sqrt((double)step);
         dx[0] = (double)step * vcur[e][0] + sq * (double)z0;
@@ -561,6 +599,7 @@ struct Walker {
 
     bool acc;
     double bn[n * n];
+    float bnf[F32 ? n * n : 1];
     if constexpr (!DRIFT) {
       if constexpr (std::is_same<R, double>::value) {
         acc = metropolis_accept(ratio, 2.0 * dJ, ubits);
@@ -585,25 +624,31 @@ struct Walker {
 #pragma unroll
         for (int j = 0; j < n; ++j) bn[k * n + j] = B[k * ld + j] - ck * (v[j] - (j == i ? 1.0 : 0.0));
       }
+      if constexpr (F32)
+#pragma unroll
+        for (int k = 0; k < n * n; ++k) bnf[k] = (float)bn[k];
       // Green's function ratio over every electron (metrop.rs:182-195) with
       // the drift at the proposed configuration
-      double hi = 0.0, lo = 0.0;
+      D hi = 0, lo = 0;
       static_for<0, N>([&](auto jc) {
         constexpr int j = decltype(jc)::value;
         constexpr bool jup = j < NU;
-        double vn[3];
+        D vn[3];
         // determinant part
         if constexpr (jup == isup) {
           constexpr int ij = jup ? j : j - NU;
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
-            double g = 0.0;
+            D g = 0;
 #pragma unroll
-            for (int k = 0; k < n; ++k) g += (double)(j == e ? o.grad[k][c] : og[j][k][c]) * bn[k * n + ij];
+            for (int k = 0; k < n; ++k) {
+              if constexpr (F32) g += (j == e ? o.grad[k][c] : og[j][k][c]) * bnf[k * n + ij];
+              else g += (double)(j == e ? o.grad[k][c] : og[j][k][c]) * bn[k * n + ij];
+            }
             vn[c] = g;
           }
         } else {
-          det_grad<j>(vn);
+          det_grad_d<j>(vn);
         }
         // Jastrow part
         R gj[3];
@@ -627,19 +672,15 @@ struct Walker {
         }
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          const double dj = (j == e) ? dx[c] : 0.0;
-          const double a = -dj - (double)step * (vn[c] + (double)gj[c]);
-          const double b = dj - (double)step * vcur[j][c];
+          const D dj = (j == e) ? (D)dx[c] : (D)0;
+          const D a = -dj - (D)step * (vn[c] + (D)gj[c]);
+          const D b = dj - (D)step * vcur[j][c];
           hi += a * a;
           lo += b * b;
         }
       });
-      const double la = 2.0 * (double)dJ - (hi - lo) / (2.0 * (double)step);
-      if constexpr (std::is_same<R, double>::value) {
-        acc = (ratio > 0.0) && metropolis_accept(ratio, la, ubits);
-      } else {
-        acc = (ratio > 0.0) && (ratio * ratio * exp(la) > (double)uacc);
-      }
+      const D la = (D)2 * (D)dJ - (hi - lo) / ((D)2 * (D)step);
+      acc = (ratio > 0.0) && metropolis_accept(ratio, (double)la, ubits);
     }
     if (!acc) return 0;
 
@@ -655,6 +696,11 @@ struct Walker {
     if constexpr (DRIFT) {
 #pragma unroll
       for (int k = 0; k < n * n; ++k) B[(k / n) * ld + (k % n)] = bn[k];
+      if constexpr (F32) {
+        float* Bf = isup ? bfu : bfd;
+#pragma unroll
+        for (int k = 0; k < n * n; ++k) Bf[(k / n) * ld + (k % n)] = bnf[k];
+      }
     } else {
       // Sherman-Morrison row update (FP64)
       double v[n], col[n];
