@@ -398,11 +398,11 @@ def dmc_leg(ctx, n_eq: int = 600, n_steps: int = 800, train_iters: int = 20) -> 
     """DMC on the Be atom (Z = 4, 2 up + 2 down, 1s/2s STO determinant):
     131,072 walkers, time step 0.005, drift-diffusion moves with Metropolis
     accept/reject, a stochastic comb every step, FP64 weights and energy
-    sums with FP32 drift and E_L (the mixed form) and the FP64 form beside it.
+    sums with FP32 drift (the mixed form) and the FP64 form beside it.
     Guides: the Pade-Jastrow fallback, and the pair-network Jastrow trained on
     Be by VMC + SR (the LiH recipe). Energies are the mean of the per-step
-    ensemble energies after n_eq steps, errors by blocking those per-step
-    energies (blocks of 20 steps)."""
+    ensemble energies after n_eq steps; the error is the larger of the
+    blocking-plateau error and the tau_corr error of those per-step energies."""
     import numpy as np
 
     from mole_gb300 import api
@@ -412,10 +412,7 @@ def dmc_leg(ctx, n_eq: int = 600, n_steps: int = 800, train_iters: int = 20) -> 
     out = {"workload": "Be DMC, 131072 walkers, tau 0.005, comb every step", "walkers": W, "tau": tau,
            "exact_ground_state": exact, "eloc_cutoff_in_weights": 2.0 / np.sqrt(tau)}
 
-    def blocked(e, b=20):
-        nb = len(e) // b
-        m = np.asarray(e[: nb * b]).reshape(nb, b).mean(1)
-        return float(m.mean()), float(m.std(ddof=1) / np.sqrt(nb)) if nb > 1 else float("nan")
+    from mole_gb300 import statistics
 
     cut = 2.0 / np.sqrt(tau)  # E_L window of the weight factor (Umrigar-Nightingale-Runge)
 
@@ -436,9 +433,11 @@ def dmc_leg(ctx, n_eq: int = 600, n_steps: int = 800, train_iters: int = 20) -> 
         wall = time.perf_counter() - t0
         ms, n = ctx.kernel_time(1)
         ctx.enable_timing(False)
-        E, err = blocked(e)
+        st = statistics.analyse(e)  # blocking plateau and tau_corr of the per-step energies
         r = {"walker_steps_per_s": W * steps / (ms * 1e-3), "ms_per_step": ms / steps,
-             "wall_ms_per_step": 1e3 * wall / steps, "energy": E, "error": err, "acceptance": dmc.acceptance,
+             "wall_ms_per_step": 1e3 * wall / steps, "energy": st["mean"],
+             "error": max(st["error"], st["error_tau"]), "tau_corr_steps": st["tau_corr"],
+             "plateau_block": st["block_size"], "acceptance": dmc.acceptance, "node_kills": dmc.node_kills,
              "steps": steps, "eq_steps": n_eq, "launches_per_step": 4}
         wk.close()
         wf.close()
