@@ -19,7 +19,7 @@ struct OgenShared {
   float w3[2][kNnH];
   float h1[kNnMaxPairs][kNnH];
   float d2[kNnMaxPairs][kNnH];
-  double x[kMaxElec * 3];
+  float x[kMaxElec * 3];  // the walker's positions (FP32: these O_k are FP32 quantities)
 };
 
 // d J_nn / d theta for one walker per CTA iteration; thread a is hidden unit a.
@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(kNnH) nn_ogen_kernel(const __grid_constant__ S
   }
   __syncthreads();
   for (int w = blockIdx.x; w < W; w += gridDim.x) {
-    if (t < 3 * N) sh.x[t] = pos[(size_t)t * W + w];
+    if (t < 3 * N) sh.x[t] = (float)pos[(size_t)t * W + w];
     __syncthreads();
     T* out = O + (size_t)w * ldO + col0;
     for (int net = 0; net < 2; ++net) {
@@ -55,20 +55,19 @@ __global__ void __launch_bounds__(kNnH) nn_ogen_kernel(const __grid_constant__ S
       const int n_b = net == 0 ? N : sp.n_nuc;
       for (int i = 0; i < N; ++i)
         for (int j = (net == 0 ? i + 1 : 0); j < n_b; ++j, ++np) {
-          double d0, d1, d2;
-          float s;
+          float d0, d1, d2, s;
           if (net == 0) {
             d0 = sh.x[3 * i] - sh.x[3 * j];
             d1 = sh.x[3 * i + 1] - sh.x[3 * j + 1];
             d2 = sh.x[3 * i + 2] - sh.x[3 * j + 2];
             s = ((i < n_up) == (j < n_up)) ? 1.f : 0.f;
           } else {
-            d0 = sh.x[3 * i] - (double)sp.nuc_pos[3 * j];
-            d1 = sh.x[3 * i + 1] - (double)sp.nuc_pos[3 * j + 1];
-            d2 = sh.x[3 * i + 2] - (double)sp.nuc_pos[3 * j + 2];
+            d0 = sh.x[3 * i] - sp.nuc_pos[3 * j];
+            d1 = sh.x[3 * i + 1] - sp.nuc_pos[3 * j + 1];
+            d2 = sh.x[3 * i + 2] - sp.nuc_pos[3 * j + 2];
             s = sp.nuc_z[j];
           }
-          const float r = (float)sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+          const float r = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
           const float er = expf(-r);
           const float x[kNnIn] = {r, er, s * r, s * er};
           // layer 1 (thread a = unit a)
@@ -78,10 +77,13 @@ __global__ void __launch_bounds__(kNnH) nn_ogen_kernel(const __grid_constant__ S
           const float h1 = tanhf(z);
           sh.h1[np][t] = h1;
           __syncthreads();
-          // layer 2 and output weight
-          float a2 = sh.b2[net][t];
-#pragma unroll 8
-          for (int c = 0; c < kNnH; ++c) a2 += sh.W2T[net][c][t] * sh.h1[np][c];
+          // layer 2 and output weight (four independent partial sums)
+          float q[4] = {sh.b2[net][t], 0.f, 0.f, 0.f};
+#pragma unroll 4
+          for (int c = 0; c < kNnH; c += 4)
+#pragma unroll
+            for (int u = 0; u < 4; ++u) q[u] += sh.W2T[net][c + u][t] * sh.h1[np][c + u];
+          const float a2 = (q[0] + q[1]) + (q[2] + q[3]);
           const float h2 = tanhf(a2);
           const float dl2 = sh.w3[net][t] * (1.f - h2 * h2);
           sh.d2[np][t] = dl2;
@@ -89,9 +91,12 @@ __global__ void __launch_bounds__(kNnH) nn_ogen_kernel(const __grid_constant__ S
           gw3 += h2;
           __syncthreads();
           // back to layer 1 (thread c = unit c)
-          float dl1 = 0.f;
-#pragma unroll 8
-          for (int a = 0; a < kNnH; ++a) dl1 += sh.W2[net][a][t] * sh.d2[np][a];
+          float r4[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 4
+          for (int a = 0; a < kNnH; a += 4)
+#pragma unroll
+            for (int u = 0; u < 4; ++u) r4[u] += sh.W2[net][a + u][t] * sh.d2[np][a + u];
+          float dl1 = (r4[0] + r4[1]) + (r4[2] + r4[3]);
           dl1 *= 1.f - h1 * h1;
           gb1 += dl1;
 #pragma unroll
@@ -152,20 +157,28 @@ cudaError_t launch_copy_cols(const double* src, int lds, int ncols, float* dst, 
 
 // ------------------------------------------------------- centre + transpose
 
-// column sums of O[W][P] (FP64) into out[P]
+// Walkers per block of the column-sum and centre-transpose kernels: sums run
+// in FP32 over one block's walkers and in FP64 (atomics, one per column and
+// block) across blocks.
+constexpr int kCtW = 256;
+
+// out[p] += scale * sum_w O[w][p] (out zeroed by the caller)
 __global__ void column_sums_kernel(const float* O, int W, int P, int ldO, double* out, double scale) {
-  __shared__ double part[8][33];
+  __shared__ float part[8][33];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  const int p = blockIdx.x * 32 + tx;
-  double s = 0.0;
+  const int p = blockIdx.x * 32 + tx, w0 = blockIdx.y * kCtW;
+  float s = 0.f;
   if (p < P)
-    for (int w = ty; w < W; w += 8) s += (double)O[(size_t)w * ldO + p];
+    for (int k = ty; k < kCtW; k += 8) {
+      const int w = w0 + k;
+      if (w < W) s += O[(size_t)w * ldO + p];
+    }
   part[ty][tx] = s;
   __syncthreads();
   if (ty == 0 && p < P) {
     double v = 0.0;
-    for (int k = 0; k < 8; ++k) v += part[k][tx];
-    out[p] = v * scale;
+    for (int k = 0; k < 8; ++k) v += (double)part[k][tx];
+    atomicAdd(&out[p], v * scale);
   }
 }
 
@@ -173,33 +186,44 @@ __global__ void column_sums_kernel(const float* O, int W, int P, int ldO, double
 __global__ void center_transpose_kernel(const float* O, int W, int P, int ldO, const double* E, const double* c,
                                         __nv_bfloat16* Ot, int K_pad, double* sumO, double* sumEO) {
   __shared__ float tile[32][33];
-  __shared__ double e_s[32];
+  __shared__ float e_s[kCtW];
+  __shared__ float red[2][8][33];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
-  const int p0 = blockIdx.x * 32, w0 = blockIdx.y * 32;
-  if (threadIdx.x < 32) e_s[threadIdx.x] = (w0 + threadIdx.x < W) ? E[w0 + threadIdx.x] : 0.0;
+  const int p0 = blockIdx.x * 32, w0 = blockIdx.y * kCtW;
+  for (int k = threadIdx.x; k < kCtW; k += blockDim.x) e_s[k] = (w0 + k < W) ? (float)E[w0 + k] : 0.f;
   const int p = p0 + tx;
-  const double cp = p < P ? c[p] : 0.0;
-  double s1 = 0.0, s2 = 0.0;
+  const float cp = p < P ? (float)c[p] : 0.f;
+  float s1 = 0.f, s2 = 0.f;
   __syncthreads();
-  for (int k = ty; k < 32; k += 8) {
-    const int w = w0 + k;
-    float v = 0.f;
-    if (p < P && w < W) {
-      const double d = (double)O[(size_t)w * ldO + p] - cp;
-      v = (float)d;
-      s1 += d;
-      s2 += e_s[k] * d;
+  for (int sub = 0; sub < kCtW; sub += 32) {
+    for (int k = ty; k < 32; k += 8) {
+      const int w = w0 + sub + k;
+      float v = 0.f;
+      if (p < P && w < W) {
+        v = O[(size_t)w * ldO + p] - cp;
+        s1 += v;
+        s2 += e_s[sub + k] * v;
+      }
+      tile[k][tx] = v;
     }
-    tile[k][tx] = v;
+    __syncthreads();
+    for (int k = ty; k < 32; k += 8) {
+      const int pp = p0 + k, w = w0 + sub + tx;
+      if (pp < P && w < W) Ot[(size_t)pp * K_pad + w] = __float2bfloat16_rn(tile[tx][k]);
+    }
+    __syncthreads();
   }
+  red[0][ty][tx] = s1;
+  red[1][ty][tx] = s2;
   __syncthreads();
-  for (int k = ty; k < 32; k += 8) {
-    const int pp = p0 + k, w = w0 + tx;
-    if (pp < P && w < W) Ot[(size_t)pp * K_pad + w] = __float2bfloat16_rn(tile[tx][k]);
-  }
-  if (p < P) {
-    atomicAdd(&sumO[p], s1);
-    atomicAdd(&sumEO[p], s2);
+  if (ty == 0 && p < P) {
+    double a = 0.0, b = 0.0;
+    for (int k = 0; k < 8; ++k) {
+      a += (double)red[0][k][tx];
+      b += (double)red[1][k][tx];
+    }
+    atomicAdd(&sumO[p], a);
+    atomicAdd(&sumEO[p], b);
   }
 }
 
@@ -207,8 +231,12 @@ cudaError_t launch_center_transpose(const float* O, int W, int P, int ldO, const
                                     bool set_center, __nv_bfloat16* Ot, int K_pad, double* sumO, double* sumEO,
                                     double* scratch, cudaStream_t s) {
   (void)scratch;
-  if (set_center) column_sums_kernel<<<(P + 31) / 32, 256, 0, s>>>(O, W, P, ldO, center, 1.0 / W);
-  dim3 grid((P + 31) / 32, (W + 31) / 32);
+  if (set_center) {
+    cudaError_t e = cudaMemsetAsync(center, 0, sizeof(double) * P, s);
+    if (e != cudaSuccess) return e;
+    column_sums_kernel<<<dim3((P + 31) / 32, (W + kCtW - 1) / kCtW), 256, 0, s>>>(O, W, P, ldO, center, 1.0 / W);
+  }
+  dim3 grid((P + 31) / 32, (W + kCtW - 1) / kCtW);
   center_transpose_kernel<<<grid, 256, 0, s>>>(O, W, P, ldO, E, center, Ot, K_pad, sumO, sumEO);
   return cudaGetLastError();
 }
