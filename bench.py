@@ -85,11 +85,11 @@ def run_case(case: str) -> None:
         b.tile = 64
         b.run(api.MetropolisGaussian(1.0), 5, 0, 1)
         r = [x.energy for x in b.run(api.MetropolisGaussian(1.0), 0, 20, 10)]
-    else:  # be-dmc
-        wf = api.WaveFunction(ctx, S.beryllium())
+    else:  # be-dmc: the DMC leg's mixed form, 131,072 walkers, 20 steps
+        wf = api.WaveFunction(ctx, S.beryllium(cusp=True))
         wk = api.Walkers(wf, 131072)
-        api.Sampler(wf, api.MetropolisDiffuse(0.005), wk).run(20, 0, 1)
-        dmc = api.DmcRunner(wf, wk, -14.6)
+        api.Sampler(wf, api.MetropolisGaussian(0.3), wk, precision=api.PREC_MIXED).run(50, 0, 1)
+        dmc = api.DmcRunner(wf, wk, -14.65, precision=api.PREC_MIXED, eloc_cutoff=2.0 / np.sqrt(0.005))
         r = dmc.run_block(0.005, 20)
     torch.cuda.synchronize()
     print(json.dumps({"case": case, "seconds": time.perf_counter() - t0,
