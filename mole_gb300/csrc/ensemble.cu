@@ -98,31 +98,65 @@ __global__ void __launch_bounds__(kScanBlock) scan_blocks_kernel(const double* w
 // One CTA: exclusive offsets of the CTA totals (in place), the comb's
 // uniform and total, this step's ensemble energy and acceptance, and the
 // step counter increment.
-__global__ void scan_totals_kernel(double* btot, int nb, const double* partials, int n_part, CombState* cs,
-                                   uint64_t* step, uint64_t seed, double* energies, int64_t e_index, int W) {
-  __shared__ double sh[4];
-  if (threadIdx.x == 0) {
-    double run = 0.0;
-    for (int b = 0; b < nb; ++b) {
-      const double t = btot[b];
-      btot[b] = run;
-      run += t;
+// One block: the exclusive scan of the per-block weight totals (block
+// offsets, in chunks of kTotThreads with a running carry), the step's sums
+// of the step-kernel partials (one warp per column), the comb's uniform and
+// the running counters.
+constexpr int kTotThreads = 512;
+__global__ void __launch_bounds__(kTotThreads) scan_totals_kernel(double* btot, int nb, const double* partials,
+                                                                  int n_part, CombState* cs, uint64_t* step,
+                                                                  uint64_t seed, double* energies, int64_t e_index,
+                                                                  int W) {
+  __shared__ double ws[kTotThreads / 32];
+  __shared__ double sums[4];
+  __shared__ double carry;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int nw = kTotThreads / 32;
+  if (threadIdx.x == 0) carry = 0.0;
+  __syncthreads();
+  for (int base = 0; base < nb; base += kTotThreads) {
+    const int i = base + threadIdx.x;
+    const double x = i < nb ? btot[i] : 0.0;
+    double v = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double t = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += t;
     }
-    cs->total = run;
-    const uint4 u = draw4(seed, 0u, (uint32_t)(*step), 0u, kTagComb);
-    cs->u = u01<double>(u.x);
+    if (lane == 31) ws[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+      double q = lane < nw ? ws[lane] : 0.0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const double t = __shfl_up_sync(0xffffffffu, q, o);
+        if (lane >= o) q += t;
+      }
+      if (lane < nw) ws[lane] = q;
+    }
+    __syncthreads();
+    const double incl = v + (warp > 0 ? ws[warp - 1] : 0.0);
+    const double c0 = carry;
+    if (i < nb) btot[i] = c0 + incl - x;  // offset of block i
+    __syncthreads();
+    if (threadIdx.x == kTotThreads - 1) carry = c0 + incl;
+    __syncthreads();
   }
-  if (threadIdx.x < 4) {  // partials rows: sum E_old, accepted, proposed, walkers on a node
-    double s = 0.0;
-    for (int r = 0; r < n_part; ++r) s += partials[(size_t)r * 4 + threadIdx.x];
-    sh[threadIdx.x] = s;
+  if (warp < 4) {  // partials rows: sum E_old, accepted, proposed, walkers on a node
+    double q = 0.0;
+    for (int r = lane; r < n_part; r += 32) q += partials[(size_t)r * 4 + warp];
+    q = warp_sum(q);
+    if (lane == 0) sums[warp] = q;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    energies[e_index] = sh[0] / ((double)W - sh[3]);  // over the walkers with weight
-    cs->accepted += sh[1];
-    cs->proposed += sh[2];
-    cs->killed += sh[3];
+    cs->total = carry;
+    const uint4 u = draw4(seed, 0u, (uint32_t)(*step), 0u, kTagComb);
+    cs->u = u01<double>(u.x);
+    energies[e_index] = sums[0] / ((double)W - sums[3]);  // over the walkers with weight
+    cs->accepted += sums[1];
+    cs->proposed += sums[2];
+    cs->killed += sums[3];
     *step += 1;
   }
 }
@@ -200,7 +234,7 @@ cudaError_t launch_comb(const double* weight, double* cum, double* btot, int nb,
                         const double* pos_in, const double* eloc_in, double* pos_out, double* eloc_out, int W, int NC,
                         cudaStream_t s) {
   scan_blocks_kernel<<<nb, kScanBlock, 0, s>>>(weight, cum, btot, W);
-  scan_totals_kernel<<<1, 32, 0, s>>>(btot, nb, partials, n_part, cs, step, seed, energies, e_index, W);
+  scan_totals_kernel<<<1, kTotThreads, 0, s>>>(btot, nb, partials, n_part, cs, step, seed, energies, e_index, W);
   comb_gather_kernel<<<(W + 127) / 128, 128, 0, s>>>(pos_in, eloc_in, pos_out, eloc_out, cum, btot, nb, cs, W, NC);
   return cudaGetLastError();
 }
