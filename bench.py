@@ -599,8 +599,14 @@ def main():
     per_launch = work.flops * ws_per_step
     achieved = per_launch / (k_ms / k_n * 1e-3) / 1e12
     peak = (fp64_peak if prec == api.PREC_FP64 else fp32_peak) / 1e3
+    # DRAM bytes per launch from the ncu capture of this kernel (profiles/vmc_kernel_h2_fp64.md,
+    # 65,536 walkers x 50 sweeps: 3.35 MB read, 0 written): the walker state is register-resident,
+    # so a launch reads the positions once whatever its sweep count
+    traffic = 3.35e6 if prec == api.PREC_FP64 else None
     roofline = {"bound": "fp64" if prec == api.PREC_FP64 else "fp32", "achieved": achieved, "peak": peak,
-                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
+                "traffic_note": "dram__bytes_read + write per launch from an ncu capture of the same kernel at "
+                                "50 sweeps; it does not grow with sweeps (register-resident walkers)",
                 "kernel": "vmc_kernel<1,1,double,2,false>" if prec == api.PREC_FP64 else "vmc_kernel<1,1,float,2,false>",
                 "kernel_ms_per_launch": k_ms / k_n, "kernel_share_of_step": k_ms / ms,
                 "host_wall_ms_per_step": 1e3 * host_s / args.steps, "step_ms": device_step_ms,
