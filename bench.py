@@ -394,7 +394,7 @@ def helium_leg(ctx) -> dict:
     return out
 
 
-def dmc_leg(ctx, n_eq: int = 600, n_steps: int = 800, train_iters: int = 20) -> dict:
+def dmc_leg(ctx, n_eq: int = 2000, n_steps: int = 800, train_iters: int = 20) -> dict:
     """DMC on the Be atom (Z = 4, 2 up + 2 down, 1s/2s STO determinant):
     131,072 walkers, time step 0.005, drift-diffusion moves with Metropolis
     accept/reject, a stochastic comb every step, FP64 weights and energy
@@ -445,7 +445,7 @@ def dmc_leg(ctx, n_eq: int = 600, n_steps: int = 800, train_iters: int = 20) -> 
 
     pade = S.beryllium(cusp=True)
     out["pade_mixed"] = run(pade, api.PREC_MIXED, n_steps, "pade")
-    out["pade_fp64"] = run(pade, api.PREC_FP64, n_steps // 2, "pade64")
+    out["pade_fp64"] = run(pade, api.PREC_FP64, n_steps, "pade64")
     m, f = out["pade_mixed"], out["pade_fp64"]
     out["pade_mixed"]["energy_delta_vs_fp64"] = m["energy"] - f["energy"]
     out["pade_mixed"]["delta_sigma"] = float(np.hypot(m["error"], f["error"]))
