@@ -42,7 +42,7 @@ def parse():
     p.add_argument("--walkers", type=int, default=65536)
     p.add_argument("--sweeps", type=int, default=2000)
     p.add_argument("--block", type=int, default=100)
-    p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    p.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "df64"])
     p.add_argument("--no-extras", action="store_true", help="skip the e2e, mixed and CPU-baseline legs")
     p.add_argument("--no-clocks", action="store_true", help="do not sample nvidia-smi during the timed region")
     p.add_argument("--case", default=None, choices=["h2-vmc", "lih-nn-vmc", "sgemm", "be-dmc", "ragged-batch"],
@@ -50,7 +50,7 @@ def parse():
     return p.parse_args()
 
 
-def run_case(case: str) -> None:
+def run_case(case: str, precision: str = "fp64") -> None:
     """Small single-purpose runs whose kernels the committed ncu summaries profile."""
     import numpy as np
     import torch
@@ -61,9 +61,10 @@ def run_case(case: str) -> None:
     ctx = api.Context(0)
     t0 = time.perf_counter()
     if case == "h2-vmc":
+        prec = {"fp64": api.PREC_FP64, "mixed": api.PREC_MIXED, "df64": api.PREC_DF64}[precision]
         wf = api.WaveFunction(ctx, S.h2(1.0, 0.5))
         wk = api.Walkers(wf, 65536)
-        samp = api.Sampler(wf, api.MetropolisGaussian(0.4), wk)
+        samp = api.Sampler(wf, api.MetropolisGaussian(0.4), wk, precision=prec)
         samp.run(20, 0, 1)
         r = samp.run(0, 50, 10, sr=True)
     elif case in ("lih-nn-vmc", "sgemm"):
@@ -131,6 +132,14 @@ class ClockSampler:
             return
         self.thread = threading.Thread(target=self._read, daemon=True)
         self.thread.start()
+        # nvidia-smi's start-up (driver and NVML initialisation) briefly stalls
+        # the GPU's host interface: wait for its first sample so that the stall
+        # falls before the timed region, then keep only later samples
+        t0 = time.perf_counter()
+        while not self.rows and time.perf_counter() - t0 < 10.0:
+            time.sleep(0.05)
+        time.sleep(0.3)
+        self.rows = []
 
     def _read(self):
         for line in self.proc.stdout:
@@ -468,6 +477,63 @@ def dmc_leg(ctx, n_eq: int = 2000, n_steps: int = 800, train_iters: int = 20) ->
     return out
 
 
+def df64_leg(ctx, wf64, make, timed, sr_step, e2e, args, W, sweeps, block, world, ws_per_step, fp64_peak) -> dict:
+    """The same H2 SR step in the FP64-accurate double-float form (every term
+    a pair of FP32 numbers on the FP32 pipe): device and end-to-end
+    throughput, the kernel's FP64-equivalent rate against the FP64 pipe's
+    peak, and its agreement with native FP64 from identical positions and
+    random streams (acceptance counts, energy and SR sums)."""
+    import numpy as np
+
+    from mole_gb300 import api, flop_model
+    from mole_gb300 import system as S
+    from mole_gb300.system import MOVE_GAUSS
+
+    wf, wk, s = make(api.PREC_DF64)
+    wf.set_parameters(wf64.parameters())
+    for _ in range(max(args.warmup, 1)):
+        sr_step(wf, s)
+    res = []
+    reruns0 = ctx.df64_reruns()
+    ctx.enable_timing(True)
+    ms = timed(lambda: res.append(sr_step(wf, s)), args.steps)
+    k_ms, k_n = ctx.kernel_time(0)
+    ctx.enable_timing(False)
+    out = {"value": world * args.steps * ws_per_step / (ms * 1e-3), "unit": "walker-steps/s",
+           "ms_per_step": ms / args.steps, "kernel_ms_per_launch": k_ms / k_n,
+           "kernel": "vmc_kernel<1,1,df64,2,false>", "energy": res[-1].energy, "energy_error": res[-1].error,
+           "dtype": "f64-accurate double-float (2 x f32, 48-bit significand)",
+           "fp64_reruns": ctx.df64_reruns() - reruns0}
+    out["e2e"] = e2e(wf, wk, s)
+    work = flop_model.walker_step(S.h2(), MOVE_GAUSS, 2, res[-1].acceptance)
+    eq = work.flops * ws_per_step / (k_ms / k_n * 1e-3) / 1e12
+    out["roofline"] = {"bound": "fp32 issue (FMA pipe)", "fp64_equivalent_tflops": eq, "fp64_peak_tflops": fp64_peak / 1e3,
+                       "fp64_equivalent_frac": eq / (fp64_peak / 1e3),
+                       "note": "algorithmic FP64 flops of the formulas (flop_model) over the kernel time: the "
+                               "double-float kernel exceeds the FP64 pipe's peak; its own bound is FP32 issue "
+                               "(profiles/vmc_kernel_h2_df64.md)"}
+    # identical positions, parameters and random streams: native FP64 against double-float
+    pos = wk.positions()
+    cmp = {}
+    for prec in (api.PREC_FP64, api.PREC_DF64):
+        w2 = api.Walkers(wf, W, seed=0x5EED + 99)
+        w2.set_positions(pos)
+        r = api.Sampler(wf, api.MetropolisGaussian(0.4), w2, precision=prec).run(0, 200, 20, sr=True)
+        cmp[prec] = (r, w2.positions())
+        w2.close()
+    a, b = cmp[api.PREC_FP64][0], cmp[api.PREC_DF64][0]
+    rel = lambda x, y: float(np.max(np.abs(np.asarray(x) - np.asarray(y)) / np.maximum(np.abs(np.asarray(y)), 1e-300)))
+    out["vs_native_fp64"] = {
+        "sweeps": 200, "walkers": W, "accepted_fp64": float(a.moments[5]), "accepted_df64": float(b.moments[5]),
+        "same_decisions": bool(a.moments[5] == b.moments[5]),
+        "energy_sum_rel": rel(b.moments[1], a.moments[1]), "energy2_sum_rel": rel(b.moments[2], a.moments[2]),
+        "sum_O_rel": rel(b.sum_O, a.sum_O), "sum_EO_rel": rel(b.sum_EO, a.sum_EO), "sum_OO_rel": rel(b.sum_OO, a.sum_OO),
+        "positions_max_abs_bohr": float(np.max(np.abs(cmp[api.PREC_DF64][1] - cmp[api.PREC_FP64][1])))}
+    wk.close()
+    wf.close()
+    return out
+
+
 def torch_sync():
     import torch
 
@@ -505,7 +571,7 @@ def run_reference(args):
 def main():
     args = parse()
     if args.case:
-        return run_case(args.case)
+        return run_case(args.case, args.precision)
     if args.impl == "reference":
         return run_reference(args)
 
@@ -523,12 +589,14 @@ def main():
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     stream = torch.cuda.current_stream()
-    prec = api.PREC_MIXED if args.precision == "mixed" else api.PREC_FP64
+    prec = {"fp64": api.PREC_FP64, "mixed": api.PREC_MIXED, "df64": api.PREC_DF64}[args.precision]
 
     ctx = api.Context(local)
     ctx.set_stream(stream.cuda_stream)
     W, sweeps, block = args.walkers, args.sweeps, args.block
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    flush.zero_()  # load the fill kernel before any timed region
+    torch.cuda.synchronize()
 
     def make(precision):
         wf = api.WaveFunction(ctx, S.h2(1.0, 0.5))
@@ -626,24 +694,29 @@ def main():
             "roofline": roofline, "clocks": clk,
             "peaks_measured": {"fp64_gflops": fp64_peak, "fp32_gflops": fp32_peak}}
 
-    if not args.no_extras:
-        # -------------------------------------------------- e2e through the C ABI
+    def e2e(wf_, wk_, sampler_) -> dict:
+        """The SR step through the C ABI with pinned host buffers: positions in
+        before and positions and sums out after every step."""
         N = 2
         host_in = torch.empty((W, N, 3), dtype=torch.float64, pin_memory=True)
         host_out = torch.empty((W, N, 3), dtype=torch.float64, pin_memory=True)
-        host_in.copy_(torch.from_numpy(wk.positions()))
+        host_in.copy_(torch.from_numpy(wk_.positions()))
         hin, hout = host_in.numpy(), host_out.numpy()
         k2 = max(3, args.steps // 2)
 
         def e2e_step():
-            wk.set_positions(hin)
-            sr_step(wf, sampler)
-            wk.wf.lib.mole_walkers_get_positions(wk.h, api.dptr(hout), hout.size)
+            wk_.set_positions(hin)
+            sr_step(wf_, sampler_)
+            wk_.wf.lib.mole_walkers_get_positions(wk_.h, api.dptr(hout), hout.size)
 
         e2e_step()
         e_ms = timed(e2e_step, k2)
-        line["e2e"] = {"value": world * k2 * ws_per_step / (e_ms * 1e-3), "unit": "walker-steps/s",
-                       "h2d_bytes_per_step": int(hin.nbytes), "d2h_bytes_per_step": int(hout.nbytes + 8 * (7 + 2 + 2 + 4))}
+        return {"value": world * k2 * ws_per_step / (e_ms * 1e-3), "unit": "walker-steps/s",
+                "h2d_bytes_per_step": int(hin.nbytes), "d2h_bytes_per_step": int(hout.nbytes + 8 * (7 + 2 + 2 + 4))}
+
+    if not args.no_extras:
+        # -------------------------------------------------- e2e through the C ABI
+        line["e2e"] = e2e(wf, wk, sampler)
         # -------------------------------------------------- mixed-precision form
         if prec == api.PREC_FP64:
             wf2, wk2, s2 = make(api.PREC_MIXED)
@@ -657,6 +730,10 @@ def main():
                              "energy": res2[-1].energy, "energy_error": res2[-1].error,
                              "energy_fp64_same_params": r_fp64.energy, "energy_fp64_error": r_fp64.error,
                              "energy_delta_vs_fp64": res2[-1].energy - r_fp64.energy}
+        # -------------------------------------------------- FP64-accurate double-float form
+        if prec == api.PREC_FP64:
+            line["fp64_accurate_df64"] = df64_leg(ctx, wf, make, timed, sr_step, e2e, args, W, sweeps, block, world,
+                                                  ws_per_step, fp64_peak)
         # -------------------------------------------------- neural vs plain, LiH
         if rank == 0 and world == 1:
             line["lih_time_to_sigma"] = lih_time_to_sigma(ctx, 16384, 20)

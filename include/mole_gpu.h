@@ -57,8 +57,14 @@ enum { MOLE_POT_COULOMB = 0, MOLE_POT_HARMONIC = 1 };
  * move with the same symmetric acceptance, MetropolisDiffuse (metrop.rs:104-217) */
 enum { MOLE_MOVE_BOX = 0, MOLE_MOVE_GAUSS = 1, MOLE_MOVE_DIFFUSE = 2 };
 /* arithmetic: all FP64, or FP32 orbital/Jastrow/MLP evaluation with FP64 inverse,
- * Sherman-Morrison ratio products, E_L and accumulation */
-enum { MOLE_PREC_FP64 = 0, MOLE_PREC_MIXED = 1 };
+ * Sherman-Morrison ratio products, E_L and accumulation, or FP64-accurate
+ * double-float: every term as a pair of FP32 numbers (48 significant bits) on
+ * the FP32 pipe, results within about 1e-13 relative of FP64. MOLE_PREC_DF64
+ * applies to box and Gaussian VMC sweeps and to mole_eval of the fixed-size
+ * families (SR sums of at most 2 parameters); a launch whose values leave
+ * FP32's exponent range is rerun in native FP64 on the device, and every other
+ * call treats MOLE_PREC_DF64 as MOLE_PREC_FP64 */
+enum { MOLE_PREC_FP64 = 0, MOLE_PREC_MIXED = 1, MOLE_PREC_DF64 = 2 };
 /* initial positions: N(0, width^2) per coordinate, or U(-width, width) as
  * Sampler::new does (src/montecarlo/src/samplers.rs:44-55) */
 enum { MOLE_INIT_NORMAL = 0, MOLE_INIT_UNIFORM = 1 };
@@ -156,6 +162,10 @@ int mole_ctx_enable_timing(mole_ctx* ctx, int32_t on);
 int mole_ctx_kernel_time(mole_ctx* ctx, int32_t kernel, double* total_ms, int64_t* launches);
 /* SM count and compute capability of the context's device (the key of tuned tiles). */
 int mole_ctx_device_info(mole_ctx* ctx, int32_t* n_sm, int32_t* cc_major, int32_t* cc_minor);
+/* Double-float (MOLE_PREC_DF64) launches of this context that were rerun in
+ * native FP64 because a value left FP32's exponent range (no reference
+ * counterpart: the reference computes in f64 only). */
+int mole_ctx_df64_reruns(mole_ctx* ctx, int64_t* reruns);
 /* Device FP64 and FP32 FMA peaks measured by a microbenchmark (GFLOP/s). */
 int mole_probe_peaks(mole_ctx* ctx, double* fp64_gflops, double* fp32_gflops);
 

@@ -31,7 +31,9 @@ from . import _lib
 from ._lib import MoleError, check, dptr
 from .system import MOVE_BOX, MOVE_DIFFUSE, MOVE_GAUSS, System
 
-PREC_FP64, PREC_MIXED = 0, 1
+# FP64; FP32 evaluation with FP64 inverse, E_L and sums; FP64-accurate
+# double-float on the FP32 pipe (box/Gaussian VMC and evaluation)
+PREC_FP64, PREC_MIXED, PREC_DF64 = 0, 1, 2
 INIT_NORMAL, INIT_UNIFORM = 0, 1
 
 
@@ -74,6 +76,12 @@ class Context:
         ms, n = C.c_double(), C.c_int64()
         check(self.lib.mole_ctx_kernel_time(self.h, kernel, C.byref(ms), C.byref(n)))
         return ms.value, n.value
+
+    def df64_reruns(self) -> int:
+        """Double-float launches rerun in native FP64 (a value left FP32's exponent range)."""
+        n = C.c_int64()
+        check(self.lib.mole_ctx_df64_reruns(self.h, C.byref(n)))
+        return n.value
 
     def probe_peaks(self) -> tuple[float, float]:
         """(FP64, FP32) FMA GFLOP/s measured on this device."""

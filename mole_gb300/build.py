@@ -64,8 +64,14 @@ def build(jobs: int | None = None, verbose: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     srcs = sources()
     jobs = jobs or max(1, os.cpu_count() or 1)
-    # the largest spin families first so the parallel build finishes sooner
-    srcs.sort(key=lambda s: -os.path.getsize(s) - (100000 if "_5_" in s or "_4_" in s else 0))
+    # the slowest translation units (largest spin families, double-float) first
+    # so the parallel build finishes sooner
+    def weight(s: str) -> int:
+        b = os.path.basename(s)
+        return (os.path.getsize(s) + 100000 * ("_2_2" in b) + 60000 * ("inst_df" in b) + 40000 * ("_2_1" in b)
+                + 200000 * (b == "capi.cu"))
+
+    srcs.sort(key=lambda s: -weight(s))
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose), srcs))
     if _stale(LIB, objs):

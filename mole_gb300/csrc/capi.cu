@@ -18,6 +18,29 @@ MOLE_DECL(1, 0)
 MOLE_DECL(1, 1)
 MOLE_DECL(2, 1)
 MOLE_DECL(2, 2)
+#define MOLE_DECL_DF(NU, ND)                      \
+  DfParts df_parts_vmc_##NU##_##ND##_0();         \
+  DfParts df_parts_vmc_##NU##_##ND##_1();         \
+  DfParts df_parts_eval_##NU##_##ND##_0();        \
+  DfParts df_parts_eval_##NU##_##ND##_1();        \
+  const KernelSetT<df64>* kernels_df_##NU##_##ND() { \
+    static const KernelSetT<df64> ks = [] {       \
+      KernelSetT<df64> k{};                       \
+      const DfParts v0 = df_parts_vmc_##NU##_##ND##_0(), v1 = df_parts_vmc_##NU##_##ND##_1(); \
+      for (int p = 0; p < kPmSlots; ++p) {        \
+        k.vmc[p][0][0] = v0.vmc[p];               \
+        k.vmc[p][0][1] = v1.vmc[p];               \
+      }                                           \
+      k.eval[0] = df_parts_eval_##NU##_##ND##_0().eval; \
+      k.eval[1] = df_parts_eval_##NU##_##ND##_1().eval; \
+      return k;                                   \
+    }();                                          \
+    return &ks;                                   \
+  }
+MOLE_DECL_DF(1, 0)
+MOLE_DECL_DF(1, 1)
+MOLE_DECL_DF(2, 1)
+MOLE_DECL_DF(2, 2)
 const NnKernelSetT<double>* nn_kernels_f64_2_2();
 const NnKernelSetT<float>* nn_kernels_f32_2_2();
 
@@ -29,6 +52,10 @@ const KernelSetT<double>* kernel_set64(int nu, int nd) {
 }
 const KernelSetT<float>* kernel_set32(int nu, int nd) {
   MOLE_CASE(1, 0, f32) MOLE_CASE(1, 1, f32) MOLE_CASE(2, 1, f32) MOLE_CASE(2, 2, f32)
+  return nullptr;
+}
+const KernelSetT<df64>* kernel_set_df(int nu, int nd) {
+  MOLE_CASE(1, 0, df) MOLE_CASE(1, 1, df) MOLE_CASE(2, 1, df) MOLE_CASE(2, 2, df)
   return nullptr;
 }
 }  // namespace mole
@@ -116,6 +143,7 @@ void fill_params(const mole_system& s, SysParams<R>& sp) {
       vnn += (double)(s.nuc_z[I] * s.nuc_z[K]) / std::sqrt(d2);
     }
   sp.vnn = vnn;
+  sp.vnn_r = (R)vnn;
   sp.nn_theta = s.d_nn_theta;
   sp.nn_tab = s.d_nn_tab;
 }
@@ -127,6 +155,7 @@ void fill_params(const mole_system& s, SysParams<R>& sp) {
 cudaError_t rebuild(mole_system& s) {
   fill_params(s, s.sp64);
   fill_params(s, s.sp32);
+  fill_params(s, s.spdf);
   if (s.nn_on && s.d_nn_theta) {
     cudaStream_t st = s.ctx->stream;
     cudaError_t e = cudaStreamSynchronize(st);
@@ -158,6 +187,13 @@ KernelSetT<float>::Vmc vmc32(const mole_system* s, int slot, int drift) {
   if (s->nn_on) return slot == 0 ? s->nk32->vmc[drift] : nullptr;
   return s->k32->vmc[slot][drift][s->en_on];
 }
+// Double-float kernels exist for the non-neural families, box and Gaussian
+// moves and SR sums of at most two parameters; NULL means "run native FP64".
+KernelSetT<df64>::Vmc vmc_df(const mole_system* s, int slot, int drift) {
+  if (s->nn_on || !s->kdf || drift) return nullptr;
+  return s->kdf->vmc[slot][0][s->en_on];
+}
+KernelSetT<df64>::Eval eval_df(const mole_system* s) { return s->nn_on || !s->kdf ? nullptr : s->kdf->eval[s->en_on]; }
 KernelSetT<double>::Eval eval64(const mole_system* s) { return s->nn_on ? s->nk64->eval : s->k64->eval[s->en_on]; }
 KernelSetT<float>::Eval eval32(const mole_system* s) { return s->nn_on ? s->nk32->eval : s->k32->eval[s->en_on]; }
 KernelSetT<double>::Dmc dmc64(const mole_system* s) { return s->nn_on ? s->nk64->dmc : s->k64->dmc[s->en_on]; }
@@ -295,6 +331,12 @@ int mole_ctx_kernel_time(mole_ctx* c, int32_t kernel, double* total_ms, int64_t*
   return MOLE_OK;
 }
 
+int mole_ctx_df64_reruns(mole_ctx* c, int64_t* reruns) {
+  if (!c || !reruns) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
+  *reruns = c->df64_reruns;
+  return MOLE_OK;
+}
+
 int mole_ctx_device_info(mole_ctx* c, int32_t* n_sm, int32_t* cc_major, int32_t* cc_minor) {
   if (!c) return fail(MOLE_ERR_INVALID_ARG, "ctx is NULL");
   int ma = 0, mi = 0;
@@ -393,6 +435,7 @@ int mole_system_create(mole_ctx* ctx, const mole_system_desc* d, const double* t
   // spin blocks without fixed-size kernels (up to 5 + 5) run in batches only
   s->k64 = kernel_set64(s->n_up, s->n_dn);
   s->k32 = kernel_set32(s->n_up, s->n_dn);
+  s->kdf = kernel_set_df(s->n_up, s->n_dn);
   if (s->nn_on) {
     s->nk64 = nn_kernels_f64_2_2();
     s->nk32 = nn_kernels_f32_2_2();
@@ -599,8 +642,19 @@ int mole_eval(mole_walkers* w, int32_t precision, double* lnpsi, double* sign, d
   CUDA_TRY(cudaMemsetAsync(c->status.p, 0, sizeof(int), c->stream));
   a.status = c->status.p;
   Timer tm(c, 2);
+  auto edf = precision == MOLE_PREC_DF64 ? eval_df(s) : nullptr;
   if (precision == MOLE_PREC_MIXED) CUDA_TRY(eval32(s)(s->sp32, a, grid_for(W), c->stream));
-  else CUDA_TRY(eval64(s)(s->sp64, a, grid_for(W), c->stream));
+  else if (edf) {
+    CUDA_TRY(edf(s->spdf, a, grid_for(W), c->stream));
+    int st = 0;
+    CUDA_TRY(cudaMemcpyAsync(&st, c->status.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (st & 8) {  // a walker outside the double-float range: evaluate all of them in FP64
+      ++c->df64_reruns;
+      CUDA_TRY(cudaMemsetAsync(c->status.p, 0, sizeof(int), c->stream));
+      CUDA_TRY(eval64(s)(s->sp64, a, grid_for(W), c->stream));
+    }
+  } else CUDA_TRY(eval64(s)(s->sp64, a, grid_for(W), c->stream));
   if (s->nn_on && O)  // the network's O_k (FP32 arithmetic) after the orbital/Pade ones
     CUDA_TRY(launch_nn_ogen64(s->sp32, w->pos, W, s->n_up, N, a.O, P, nwalker_par, std::min(W, 3 * c->n_sm),
                               c->stream));
@@ -646,6 +700,7 @@ int mole_vmc_run(mole_walkers* w, const mole_vmc_opts* o, double* moments, doubl
   const bool mixed = o->precision == MOLE_PREC_MIXED;
   auto f64 = vmc64(s, slot, drift);
   auto f32 = vmc32(s, slot, drift);
+  auto fdf = o->precision == MOLE_PREC_DF64 ? vmc_df(s, slot, drift) : nullptr;
   if (mixed ? !f32 : !f64) return fail(MOLE_ERR_UNSUPPORTED, "SR kernel not compiled for this family and precision");
   int wpc = kBlock;
   const int W = w->W, grid = vmc_grid(W, s->n_up, s->n_dn, c->n_sm, &wpc), NA = n_acc(PM);
@@ -669,10 +724,31 @@ int mole_vmc_run(mole_walkers* w, const mole_vmc_opts* o, double* moments, doubl
   a.partials = c->partials.p;
   a.tb_partials = c->tb_partials.p;
   a.status = c->status.p;
+  const size_t pos_n = (size_t)3 * (s->n_up + s->n_dn) * W;
+  if (fdf) {
+    CUDA_TRY(c->pos_backup.reserve(pos_n));
+    CUDA_TRY(cudaMemcpyAsync(c->pos_backup.p, w->pos, sizeof(double) * pos_n, cudaMemcpyDeviceToDevice, c->stream));
+  }
   Timer tm(c, 0);
   if (mixed) CUDA_TRY(f32(s->sp32, a, grid, c->stream));
+  else if (fdf) CUDA_TRY(fdf(s->spdf, a, grid, c->stream));
   else CUDA_TRY(f64(s->sp64, a, grid, c->stream));
   tm.stop();
+  if (fdf) {
+    int st = 0;
+    CUDA_TRY(cudaMemcpyAsync(&st, c->status.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (st & 8) {
+      // a value left FP32's exponent range: the same sweeps again in native
+      // FP64 from the same positions and random streams
+      ++c->df64_reruns;
+      CUDA_TRY(cudaMemcpyAsync(w->pos, c->pos_backup.p, sizeof(double) * pos_n, cudaMemcpyDeviceToDevice, c->stream));
+      CUDA_TRY(cudaMemsetAsync(c->status.p, 0, sizeof(int), c->stream));
+      Timer tm2(c, 0);
+      CUDA_TRY(f64(s->sp64, a, grid, c->stream));
+      tm2.stop();
+    }
+  }
   CUDA_TRY(launch_reduce_columns(c->partials.p, grid, NA, c->reduced.p, c->stream));
   if (n_tb > 0) CUDA_TRY(launch_reduce_columns(c->tb_partials.p, grid, n_tb, c->reduced.p + NA, c->stream));
   std::vector<double> h((size_t)NA + std::max(n_tb, 0));

@@ -61,8 +61,26 @@ typename KernelSetT<R>::Dmc maybe_dmc() {
     return &ks;                                                                                          \
   }
 
+// Double-float (FP64-accurate) kernels: box and Gaussian VMC and evaluation;
+// drift-diffusion moves and DMC stay native FP64. Each family's launchers are
+// compiled in three translation units (VMC without and with the e-n term,
+// evaluation) so that the build runs them in parallel.
+struct DfParts {
+  KernelSetT<df64>::Vmc vmc[kPmSlots];  // [PM slot]; slot 2 (eight-wide SR) not compiled
+  KernelSetT<df64>::Eval eval;
+};
+#define MOLE_INSTANTIATE_DF_VMC(NU, ND, EN)                                                   \
+  DfParts df_parts_vmc_##NU##_##ND##_##EN() {                                                \
+    return DfParts{{launch_vmc<NU, ND, df64, 0, false, EN>, launch_vmc<NU, ND, df64, 2, false, EN>, nullptr}, \
+                   nullptr};                                                                 \
+  }
+#define MOLE_INSTANTIATE_DF_EVAL(NU, ND)                                                      \
+  DfParts df_parts_eval_##NU##_##ND##_0() { return DfParts{{}, launch_eval<NU, ND, df64, false>}; } \
+  DfParts df_parts_eval_##NU##_##ND##_1() { return DfParts{{}, launch_eval<NU, ND, df64, true>}; }
+
 const KernelSetT<double>* kernel_set64(int nu, int nd);
 const KernelSetT<float>* kernel_set32(int nu, int nd);
+const KernelSetT<df64>* kernel_set_df(int nu, int nd);
 
 // Neural-Jastrow kernels (e-n terms on; the weights in dynamic shared memory).
 template <class R>

@@ -54,6 +54,8 @@ struct mole_ctx {
   int64_t kernel_launches[mole::kTimeSlots] = {};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   DevBuf<double> partials, tb_partials, reduced, scratch;
+  DevBuf<double> pos_backup;  // positions before a double-float launch (its native rerun starts there)
+  int64_t df64_reruns = 0;    // double-float launches rerun in native FP64
   DevBuf<int> status;
   int refs = 1;
   bool closed = false;
@@ -71,8 +73,10 @@ struct mole_system {
   std::vector<double> theta;
   SysParams<double> sp64;
   SysParams<float> sp32;
+  SysParams<df64> spdf;
   const KernelSetT<double>* k64 = nullptr;
   const KernelSetT<float>* k32 = nullptr;
+  const KernelSetT<df64>* kdf = nullptr;  // double-float kernels (NULL where not compiled)
   const NnKernelSetT<double>* nk64 = nullptr;  // neural systems
   const NnKernelSetT<float>* nk32 = nullptr;
   double* d_nn_theta = nullptr;  // device copy of the network parameters

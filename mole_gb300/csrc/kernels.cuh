@@ -48,7 +48,7 @@ struct VmcArgs {
   int wpc;              // walkers per CTA (<= blockDim.x): CTA b runs walkers [b wpc, (b + 1) wpc)
   double* partials;     // [gridDim.x][n_acc]
   double* tb_partials;  // [gridDim.x][n_steps / block_size]
-  int* status;          // bit 0: non-finite E_L; bit 1: singular determinant
+  int* status;          // bit 0: non-finite E_L; bit 1: singular determinant; bit 3: df64 range left
 };
 
 // The energy sums live in registers; the SR sums, touched once per sweep,
@@ -73,11 +73,14 @@ __device__ __forceinline__ NnCtx<R> nn_setup(const SysParams<R>& sp) {
 template <int NU, int ND, class R, int PM, bool EN, bool NN, int MOVE>
 __device__ __forceinline__ void vmc_body(const SysParams<R>& sp, const VmcArgs& a, double* red, double* srs) {
   using Wk = Walker<NU, ND, R, PM, EN, NN>;
+  using F = typename Wk::F;  // accumulation type: double, or df64 in the double-float form
   constexpr int NA = n_acc(PM);
   constexpr int NSR = NA - kNMom;
   const int w = blockIdx.x * a.wpc + threadIdx.x;
   const int tid = threadIdx.x;
   const bool active = tid < a.wpc && w < a.W;
+  if constexpr (Wk::DF) df64_setup();
+  F* srf = reinterpret_cast<F*>(srs);  // df64 is 8 bytes like the double slots
   Wk wk;
   wk.nn = nn_setup<R, NN>(sp);
   if (active) wk.load(a.pos, a.W, w);
@@ -85,10 +88,11 @@ __device__ __forceinline__ void vmc_body(const SysParams<R>& sp, const VmcArgs& 
 #pragma unroll
     for (int e = 0; e < Wk::N; ++e) wk.x[e][0] = wk.x[e][1] = wk.x[e][2] = 1.0 + e;
   bool ok = wk.refresh(sp, nullptr, nullptr);
-  double sE = 0.0, sE2 = 0.0, sB2 = 0.0, bsum = 0.0;
+  F sE = F(0), sE2 = F(0), bsum = F(0);
+  double sB2 = 0.0;
   int naccept = 0;
 #pragma unroll
-  for (int k = 0; k < NSR; ++k) srs[k * kBlock + tid] = 0.0;
+  for (int k = 0; k < NSR; ++k) srf[k * kBlock + tid] = F(0);
   const int total = a.n_eq + a.n_steps;
   const int refresh = a.refresh > 0 ? a.refresh : 100;
   const R step = (R)a.step;
@@ -97,8 +101,8 @@ __device__ __forceinline__ void vmc_body(const SysParams<R>& sp, const VmcArgs& 
     naccept += wk.template sweep<MOVE>(sp, step, a.seed, (uint32_t)w, t);
     if ((it + 1) % refresh == 0) ok = wk.refresh(sp, nullptr, nullptr) && ok;
     if (it < a.n_eq) continue;
-    double O[PM > 0 ? PM : 1];
-    const double E = wk.local_energy(sp, O, nullptr, nullptr);
+    F O[PM > 0 ? PM : 1];
+    const F E = wk.local_energy(sp, O, nullptr, nullptr);
     const int k = it - a.n_eq;
     sE += E;
     sE2 += E * E;
@@ -106,30 +110,35 @@ __device__ __forceinline__ void vmc_body(const SysParams<R>& sp, const VmcArgs& 
     if constexpr (PM > 0) {
 #pragma unroll
       for (int p = 0; p < PM; ++p) {
-        srs[p * kBlock + tid] += O[p];
-        srs[(PM + p) * kBlock + tid] += E * O[p];
+        srf[p * kBlock + tid] += O[p];
+        srf[(PM + p) * kBlock + tid] += E * O[p];
       }
       int q = 2 * PM;
 #pragma unroll
       for (int p = 0; p < PM; ++p)
 #pragma unroll
-        for (int r = p; r < PM; ++r, ++q) srs[q * kBlock + tid] += O[p] * O[r];
+        for (int r = p; r < PM; ++r, ++q) srf[q * kBlock + tid] += O[p] * O[r];
     }
     if ((k + 1) % a.block_size == 0) {
-      const double m = bsum / a.block_size;
+      const double bs = to_d(bsum);
+      const double m = bs / a.block_size;
       sB2 += m * m;
-      double v[1] = {active ? bsum : 0.0};
+      double v[1] = {active ? bs : 0.0};
       block_sum<1>(v, red);
       if (threadIdx.x == 0) a.tb_partials[(size_t)blockIdx.x * (a.n_steps / a.block_size) + k / a.block_size] = v[0];
-      bsum = 0.0;
+      bsum = F(0);
     }
   }
-  double acc[kNMom] = {(double)a.n_steps, sE, sE2, sB2, (double)(a.n_steps / a.block_size), (double)naccept,
+  const double dE = to_d(sE), dE2 = to_d(sE2);
+  double acc[kNMom] = {(double)a.n_steps, dE, dE2, sB2, (double)(a.n_steps / a.block_size), (double)naccept,
                        (double)total * Wk::N};
   if (active) {
     wk.store(a.pos, a.W, w);
-    if (!ok) atomicOr(a.status, 2);
-    if (!(sE == sE) || !(sE2 < 1e300)) atomicOr(a.status, 1);
+    // the df64 form reports every anomaly as out of range: the host reruns
+    // the launch in native FP64, which reports its own status
+    if (!ok) atomicOr(a.status, Wk::DF ? 8 : 2);
+    if (!(dE == dE) || !(dE2 < 1e300)) atomicOr(a.status, Wk::DF ? 8 : 1);
+    if (Wk::DF && wk.oor) atomicOr(a.status, 8);
   } else {
 #pragma unroll
     for (int k = 0; k < kNMom; ++k) acc[k] = 0.0;
@@ -137,7 +146,7 @@ __device__ __forceinline__ void vmc_body(const SysParams<R>& sp, const VmcArgs& 
   // deterministic CTA reduction, then one partial row per CTA
 #pragma unroll
   for (int k = 0; k < NA; ++k) {
-    double v[1] = {k < kNMom ? acc[k] : (active ? srs[(k - kNMom) * kBlock + tid] : 0.0)};
+    double v[1] = {k < kNMom ? acc[k] : (active ? to_d(srf[(k - kNMom) * kBlock + tid]) : 0.0)};
     block_sum<1>(v, red);
     if (threadIdx.x == 0) a.partials[(size_t)blockIdx.x * NA + k] = v[0];
   }
@@ -176,18 +185,21 @@ template <int NU, int ND, class R, int PM, bool EN, bool NN = false>
 __global__ void __launch_bounds__(kBlock) eval_kernel(const __grid_constant__ SysParams<R> sp, const EvalArgs a) {
   using Wk = Walker<NU, ND, R, PM, EN, NN>;
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if constexpr (Wk::DF) df64_setup();
   Wk wk;
   wk.nn = nn_setup<R, NN>(sp);
   if (w >= a.W) return;
   wk.load(a.pos, a.W, w);
   double ln, sg;
   const bool ok = wk.refresh(sp, &ln, &sg);
-  double O[PM > 0 ? PM : 1];
+  typename Wk::F O[PM > 0 ? PM : 1];
   double g[Wk::N * 3];
   double lap;
-  const double E = wk.local_energy(sp, O, g, &lap);
-  if (!ok) atomicOr(a.status, 2);
-  if (!(E == E)) atomicOr(a.status, 1);
+  const double E = to_d(wk.local_energy(sp, O, g, &lap));
+  // the df64 form reports every anomaly as out of range (the host reruns in FP64)
+  if (!ok) atomicOr(a.status, Wk::DF ? 8 : 2);
+  if (!(E == E)) atomicOr(a.status, Wk::DF ? 8 : 1);
+  if (Wk::DF && wk.oor) atomicOr(a.status, 8);
   a.lnpsi[w] = ln;
   a.sign[w] = sg;
   a.lap[w] = lap;
@@ -196,7 +208,7 @@ __global__ void __launch_bounds__(kBlock) eval_kernel(const __grid_constant__ Sy
   for (int k = 0; k < Wk::N * 3; ++k) a.grad[(size_t)w * Wk::N * 3 + k] = g[k];
   if constexpr (PM > 0)
     if (a.O)
-      for (int p = 0; p < sp.P && p < PM && p < a.ldO; ++p) a.O[(size_t)w * a.ldO + p] = O[p];
+      for (int p = 0; p < sp.P && p < PM && p < a.ldO; ++p) a.O[(size_t)w * a.ldO + p] = to_d(O[p]);
 }
 
 struct DmcArgs {

@@ -12,12 +12,14 @@
 // after a sweep is assembled from the caches without a single exp, sqrt or
 // division.
 //
-// Arithmetic type R is double (plain method) or float (mixed method). The
-// inverse matrices, the Sherman-Morrison ratio products, the local-energy
-// assembly and every accumulation are FP64 in both.
+// Arithmetic type R is double (plain method), float (mixed method) or df64
+// (FP64-accurate double-float on the FP32 pipe). The inverse matrices, the
+// Sherman-Morrison ratio products, the local-energy assembly and every
+// accumulation are FP64 for double and float, and df64 for df64 (type F).
 #pragma once
 
 #include "common.cuh"
+#include "df64.cuh"
 #include "nn.cuh"
 #include "normal.cuh"
 
@@ -45,6 +47,7 @@ struct SysParams {
   int pot_kind;  // 0 Coulomb, 1 harmonic
   R half_omega2;
   double vnn;  // n-n repulsion constant
+  R vnn_r;     // the same in R (read by the df64 form)
   int n_exp, P, off_ee, off_en, off_nn;
   const double* nn_theta;  // device copy of the 9,090 network parameters (neural systems)
   const float* nn_tab;     // quintic tables of the pair networks (neural systems, FP32 form)
@@ -60,6 +63,10 @@ template <>
 __device__ __forceinline__ float rsqrt_t<float>(float x) {
   return rsqrtf(x);
 }
+template <>
+__device__ __forceinline__ df64 rsqrt_t<df64>(df64 x) {
+  return df_rsqrt(x);
+}
 template <class R>
 __device__ __forceinline__ R exp_t(R x);
 template <>
@@ -69,6 +76,10 @@ __device__ __forceinline__ double exp_t<double>(double x) {
 template <>
 __device__ __forceinline__ float exp_t<float>(float x) {
   return __expf(x);
+}
+template <>
+__device__ __forceinline__ df64 exp_t<df64>(df64 x) {
+  return df_exp(x);
 }
 
 // One electron's orbitals of its spin block (value, gradient, Laplacian),
@@ -111,6 +122,7 @@ __device__ __forceinline__ void one_body(const SysParams<R>& sp, int spin, const
   o.ljen = 0;
   o.djen = 0;
   o.ven = 0;
+  #pragma unroll 1
   for (int I = 0; I < sp.n_nuc; ++I) {
     const R d0 = r[0] - sp.nuc_pos[3 * I], d1 = r[1] - sp.nuc_pos[3 * I + 1], d2 = r[2] - sp.nuc_pos[3 * I + 2];
     const R r2 = d0 * d0 + d1 * d1 + d2 * d2;
@@ -118,6 +130,7 @@ __device__ __forceinline__ void one_body(const SysParams<R>& sp, int spin, const
     const R rr = r2 * inv;
     o.ven -= sp.nuc_z[I] * inv;
     const int b1 = sp.nuc_b0[I + 1];
+    #pragma unroll 1
     for (int b = sp.nuc_b0[I]; b < b1; ++b) {
       const int kind = sp.b_kind[b];
       const R z = sp.b_zeta[b];
@@ -239,6 +252,7 @@ __device__ __forceinline__ void pair_vals(const SysParams<R>& sp, bool same, R d
   R uRR = (R)-2 * cusp * sp.ee_b * q * q * q;
   if constexpr (PM > 0) v.db = -cusp * Rs * Rs * q * q;
   R Rk = Rs, Rk2 = 1;  // R^(p-1), R^(p-2)
+  #pragma unroll 1
   for (int i = 0; i < sp.ee_npoly; ++i) {
     const R p = (R)(i + 2), c = sp.ee_poly[i];
     val += c * Rk * Rs;
@@ -273,23 +287,40 @@ __device__ __forceinline__ bool metropolis_accept(double ratio, double x, uint32
   }
   return ratio * ratio * exp(x) > u01<double>(ubits);
 }
+// The same test for double-float ratio and exponent: the high words are the
+// values rounded to FP32, so the screen above holds unchanged; borderline
+// cases decide in FP64 on the double-float values.
+__device__ __forceinline__ bool metropolis_accept(df64 ratio, df64 x, uint32_t ubits) {
+  const float r2 = ratio.h * ratio.h;
+  if (fabsf(x.h) < 80.f && r2 > 1e-30f && r2 < 1e30f) {
+    const float uf = u01<float>(ubits);
+    const float d = r2 * __expf(x.h) - uf;
+    if (fabsf(d) > 1e-3f * uf) return d > 0.f;
+  }
+  const double rd = (double)ratio;
+  return rd * rd * exp((double)x) > u01<double>(ubits);
+}
+
+// Pivot magnitude of the Gauss-Jordan elimination.
+__device__ __forceinline__ double piv_mag(double x) { return fabs(x); }
+__device__ __forceinline__ float piv_mag(df64 x) { return fabsf(x.h); }
 
 // In-register Gauss-Jordan inverse with partial pivoting; row swaps are
 // predicated so that every index stays compile-time.
-template <int n>
-__device__ __forceinline__ bool gj_invert(double (&a)[n * n], double (&inv)[n * n], double* lndet, double* sign) {
+template <int n, class T>
+__device__ __forceinline__ bool gj_invert(T (&a)[n * n], T (&inv)[n * n], double* lndet, double* sign) {
 #pragma unroll
-  for (int i = 0; i < n * n; ++i) inv[i] = (i / n == i % n) ? 1.0 : 0.0;
+  for (int i = 0; i < n * n; ++i) inv[i] = (i / n == i % n) ? T(1) : T(0);
   double ld = 0.0, sg = 1.0;
   bool ok = true;
 #pragma unroll
   for (int col = 0; col < n; ++col) {
     int piv = col;
-    double best = fabs(a[col * n + col]);
+    auto best = piv_mag(a[col * n + col]);
 #pragma unroll
     for (int r = col + 1; r < n; ++r)
-      if (fabs(a[r * n + col]) > best) {
-        best = fabs(a[r * n + col]);
+      if (piv_mag(a[r * n + col]) > best) {
+        best = piv_mag(a[r * n + col]);
         piv = r;
       }
 #pragma unroll
@@ -297,7 +328,7 @@ __device__ __forceinline__ bool gj_invert(double (&a)[n * n], double (&inv)[n * 
       if (r == piv) {
 #pragma unroll
         for (int j = 0; j < n; ++j) {
-          double t = a[col * n + j];
+          T t = a[col * n + j];
           a[col * n + j] = a[r * n + j];
           a[r * n + j] = t;
           t = inv[col * n + j];
@@ -306,11 +337,11 @@ __device__ __forceinline__ bool gj_invert(double (&a)[n * n], double (&inv)[n * 
         }
         sg = -sg;
       }
-    const double p = a[col * n + col];
-    ok = ok && (p != 0.0);
-    if (lndet) ld += log(fabs(p));
-    if (p < 0.0) sg = -sg;
-    const double ip = 1.0 / p;
+    const T p = a[col * n + col];
+    ok = ok && !is_zero(p);
+    if (lndet) ld += log(fabs(to_d(p)));
+    if (is_neg(p)) sg = -sg;
+    const T ip = recip(p);
 #pragma unroll
     for (int j = 0; j < n; ++j) {
       a[col * n + j] *= ip;
@@ -319,7 +350,7 @@ __device__ __forceinline__ bool gj_invert(double (&a)[n * n], double (&inv)[n * 
 #pragma unroll
     for (int r = 0; r < n; ++r) {
       if (r == col) continue;
-      const double f = a[r * n + col];
+      const T f = a[r * n + col];
 #pragma unroll
       for (int j = 0; j < n; ++j) {
         a[r * n + j] -= f * a[col * n + j];
@@ -348,15 +379,21 @@ struct Walker {
   static constexpr int NZ = PM == 0 ? 0 : (PM == 2 ? 1 : PM);
   static constexpr int NZC = NZ > 0 ? NZ : 1;
   using SP = SysParams<R>;
+  // FP64-part type: double, or df64 in the double-float form
+  static constexpr bool DF = is_df64<R>::value;
+  using F = typename std::conditional<DF, df64, double>::type;
 
-  double x[N][3];
-  double bu[NU * NU];    // inverse of the up Slater matrix, bu[k*NU+i]
-  double bd[NDm * NDm];  // inverse of the down Slater matrix
+  F x[N][3];
+  F bu[NU * NU];    // inverse of the up Slater matrix, bu[k*NU+i]
+  F bd[NDm * NDm];  // inverse of the down Slater matrix
+  // df64 form: set when a value left the range where double-float keeps
+  // FP64 accuracy (the launch is then rerun in native FP64)
+  bool oor = false;
   // The FP32 form's drift-diffusion move computes drifts and Green's-function
   // sums in FP32 from an FP32 copy of the inverses (set at every refresh and
   // every accepted drift move); ratios and updates stay on the FP64 ones.
   static constexpr bool F32 = std::is_same<R, float>::value;
-  using D = typename std::conditional<F32, float, double>::type;  // drift arithmetic
+  using D = typename std::conditional<F32, float, F>::type;  // drift arithmetic
   float bfu[F32 ? NU * NU : 1];
   float bfd[F32 ? NDm * NDm : 1];
   // one-body caches
@@ -375,13 +412,13 @@ struct Walker {
 #pragma unroll
     for (int e = 0; e < N; ++e)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) x[e][c] = pos[(size_t)(3 * e + c) * W + w];
+      for (int c = 0; c < 3; ++c) x[e][c] = F(pos[(size_t)(3 * e + c) * W + w]);
   }
   __device__ __forceinline__ void store(double* pos, int W, int w) const {
 #pragma unroll
     for (int e = 0; e < N; ++e)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) pos[(size_t)(3 * e + c) * W + w] = x[e][c];
+      for (int c = 0; c < 3; ++c) pos[(size_t)(3 * e + c) * W + w] = to_d(x[e][c]);
   }
   __device__ __forceinline__ void rpos(int e, R (&r)[3]) const {
     r[0] = (R)x[e][0];
@@ -423,7 +460,7 @@ struct Walker {
   // Rebuilds the inverses in FP64 from fresh orbital values and every cache.
   // Returns false on a singular block.
   __device__ bool refresh(const SP& sp, double* lndet, double* sign) {
-    double au[NU * NU], ad[NDm * NDm];
+    F au[NU * NU], ad[NDm * NDm];
     static_for<0, N>([&](auto ec) {
       constexpr int e = decltype(ec)::value;
       constexpr bool isup = e < NU;
@@ -435,8 +472,8 @@ struct Walker {
       one_body<R, n, NZ, EN, NN>(sp, isup ? 0 : 1, r, o, &nn);
 #pragma unroll
       for (int k = 0; k < n; ++k) {
-        if constexpr (isup) au[i * NU + k] = (double)o.val[k];
-        else ad[i * NDm + k] = (double)o.val[k];
+        if constexpr (isup) au[i * NU + k] = (F)o.val[k];
+        else ad[i * NDm + k] = (F)o.val[k];
       }
       put_one_body<e, n>(o);
     });
@@ -449,9 +486,10 @@ struct Walker {
 #pragma unroll
       for (int k = 0; k < (ND > 0 ? ND * ND : 0); ++k) bfd[k] = (float)bd[k];
     }
-    double J = 0.0;
+    if constexpr (DF) check_range<NU>(bu), check_range<ND>(bd);
+    F J = F(0);
 #pragma unroll
-    for (int e = 0; e < N; ++e) J += (double)jen[e];
+    for (int e = 0; e < N; ++e) J += (F)jen[e];
     static_for<0, N>([&](auto ic) {
       constexpr int i = decltype(ic)::value;
       static_for<i + 1, N>([&](auto jc) {
@@ -460,27 +498,39 @@ struct Walker {
         pair_vals<R, PM, NN>(sp, same_spin(i, j), (R)(x[i][0] - x[j][0]), (R)(x[i][1] - x[j][1]),
                              (R)(x[i][2] - x[j][2]), v, &nn);
         put_pair(pidx(i, j), v);
-        J += (double)v.u;
+        J += (F)v.u;
       });
     });
-    if (lndet) *lndet = l1 + l2 + J;
+    if (lndet) *lndet = l1 + l2 + to_d(J);
     if (sign) *sign = s1 * s2;
     return ok;
   }
 
+  // df64 form: inverse entries beyond 2^96 mean orbital values near the
+  // bottom of FP32's exponent range, where double-float loses digits
+  template <int n, class B>
+  __device__ __forceinline__ void check_range(const B& b) {
+    if constexpr (n > 0) {
+      bool in = true;  // NaN compares false, so it counts as out of range
+#pragma unroll
+      for (int k = 0; k < n * n; ++k) in = in && (piv_mag(b[k]) < 0x1p96f);
+      if (!in) oor = true;
+    }
+  }
+
   // grad ln det at electron j from the caches and the inverse B
   template <int j>
-  __device__ __forceinline__ void det_grad(double (&g)[3]) const {
+  __device__ __forceinline__ void det_grad(F (&g)[3]) const {
     constexpr bool isup = j < NU;
     constexpr int n = isup ? NU : ND;
     constexpr int i = isup ? j : j - NU;
     constexpr int ld = isup ? NU : NDm;
-    const double* B = isup ? bu : bd;
+    const F* B = isup ? bu : bd;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      double s = 0.0;
+      F s = F(0);
 #pragma unroll
-      for (int k = 0; k < n; ++k) s += (double)og[j][k][c] * B[k * ld + i];
+      for (int k = 0; k < n; ++k) s += (F)og[j][k][c] * B[k * ld + i];
       g[c] = s;
     }
   }
@@ -528,7 +578,8 @@ struct Walker {
     constexpr int i = isup ? e : e - NU;
     constexpr bool DRIFT = MOVE == kMoveDiffuse;
     constexpr int ld = isup ? NU : NDm;
-    double* B = isup ? bu : bd;
+    static_assert(!(DF && DRIFT), "the df64 form has no drift-diffusion kernel");
+    F* B = isup ? bu : bd;
 
     // drift at the current configuration (diffuse moves)
     D vcur[N][3];
@@ -545,13 +596,13 @@ struct Walker {
     }
 
     const uint4 ra = draw4(seed, wid, t, 2u * e, kTagMove);
-    double dx[3];
+    F dx[3];
     R uacc;
     uint32_t ubits;
     if constexpr (MOVE == kMoveBox) {
-      dx[0] = (double)(step * (u01<R>(ra.x) - (R)0.5));
-      dx[1] = (double)(step * (u01<R>(ra.y) - (R)0.5));
-      dx[2] = (double)(step * (u01<R>(ra.z) - (R)0.5));
+      dx[0] = (F)(step * (u01<R>(ra.x) - (R)0.5));
+      dx[1] = (F)(step * (u01<R>(ra.y) - (R)0.5));
+      dx[2] = (F)(step * (u01<R>(ra.z) - (R)0.5));
       uacc = u01<R>(ra.w);
       ubits = ra.w;
     } else {
@@ -561,7 +612,11 @@ struct Walker {
       const uint4 rb = draw4(seed, wid, t, 2u * e + 1u, kTagMove);
       uacc = u01<R>(rb.x);
       ubits = rb.x;
-      if constexpr (MOVE == kMoveGauss) {
+      if constexpr (MOVE == kMoveGauss && DF) {
+        dx[0] = df_mul(step, z0);
+        dx[1] = df_mul(step, z1);
+        dx[2] = df_mul(step, z2);
+      } else if constexpr (MOVE == kMoveGauss) {
         dx[0] = (double)step * (double)z0;
         dx[1] = (double)step * (double)z1;
         dx[2] = (double)step * (double)z2;
@@ -577,13 +632,13 @@ struct Walker {
         dx[2] = (double)step * vcur[e][2] + sq * (double)z2;
       }
     }
-    const double xn[3] = {x[e][0] + dx[0], x[e][1] + dx[1], x[e][2] + dx[2]};
+    const F xn[3] = {x[e][0] + dx[0], x[e][1] + dx[1], x[e][2] + dx[2]};
     const R rn[3] = {(R)xn[0], (R)xn[1], (R)xn[2]};
     OneBody<R, n, NZ> o;
     one_body<R, n, NZ, EN, NN>(sp, isup ? 0 : 1, rn, o, &nn);
-    double ratio = 0.0;
+    F ratio = F(0);
 #pragma unroll
-    for (int k = 0; k < n; ++k) ratio += (double)o.val[k] * B[k * ld + i];
+    for (int k = 0; k < n; ++k) ratio += (F)o.val[k] * B[k * ld + i];
 
     // new pair terms of electron e
     R dJ = o.jen - jen[e];
@@ -598,11 +653,13 @@ struct Walker {
     });
 
     bool acc;
-    double bn[n * n];
+    F bn[n * n];
     float bnf[F32 ? n * n : 1];
     if constexpr (!DRIFT) {
       if constexpr (std::is_same<R, double>::value) {
         acc = metropolis_accept(ratio, 2.0 * dJ, ubits);
+      } else if constexpr (DF) {
+        acc = metropolis_accept(ratio, twice(dJ), ubits);
       } else {
         const double p = ratio * ratio * (double)exp_t<R>((R)2 * dJ);
         acc = p > (double)uacc;
@@ -703,21 +760,29 @@ struct Walker {
       }
     } else {
       // Sherman-Morrison row update (FP64)
-      double v[n], col[n];
+      F v[n], col[n];
 #pragma unroll
       for (int j = 0; j < n; ++j) {
-        double s = 0.0;
+        F s = F(0);
 #pragma unroll
-        for (int k = 0; k < n; ++k) s += (double)o.val[k] * B[k * ld + j];
+        for (int k = 0; k < n; ++k) s += (F)o.val[k] * B[k * ld + j];
         v[j] = s;
       }
-      const double ir = 1.0 / ratio;
+      const F ir = recip(ratio);
 #pragma unroll
       for (int k = 0; k < n; ++k) col[k] = B[k * ld + i] * ir;
 #pragma unroll
       for (int k = 0; k < n; ++k)
 #pragma unroll
-        for (int j = 0; j < n; ++j) B[k * ld + j] -= col[k] * (v[j] - (j == i ? 1.0 : 0.0));
+        for (int j = 0; j < n; ++j) B[k * ld + j] -= col[k] * (v[j] - (j == i ? F(1) : F(0)));
+      if constexpr (DF) {
+        bool in = true;
+#pragma unroll
+        for (int k = 0; k < n; ++k)
+#pragma unroll
+          for (int j = 0; j < n; ++j) in = in && (piv_mag(B[k * ld + j]) < 0x1p96f);
+        if (!in) oor = true;
+      }
     }
     return 1;
   }
@@ -733,71 +798,73 @@ struct Walker {
   // assembled from the caches. With PM > 0 also O_k = d ln psi / d theta_k
   // for the first PM parameters. grad (optional) receives grad ln psi [N][3];
   // lapout receives sum_i lap_i psi / psi.
-  __device__ double local_energy(const SP& sp, double (&O)[PMC], double* grad, double* lapout) const {
-    double lap = 0.0, V = 0.0;
+  __device__ F local_energy(const SP& sp, F (&O)[PMC], double* grad, double* lapout) const {
+    F lap = F(0), V = F(0);
     if constexpr (PM > 0)
 #pragma unroll
-      for (int p = 0; p < PM; ++p) O[p] = 0.0;
-    double djs = 0.0;
+      for (int p = 0; p < PM; ++p) O[p] = F(0);
+    F djs = F(0);
     static_for<0, N>([&](auto ec) {
       constexpr int e = decltype(ec)::value;
       constexpr bool isup = e < NU;
       constexpr int n = isup ? NU : ND;
       constexpr int i = isup ? e : e - NU;
       constexpr int ld = isup ? NU : NDm;
-      const double* B = isup ? bu : bd;
-      double gD[3], lD = 0.0;
+      const F* B = isup ? bu : bd;
+      F gD[3], lD = F(0);
       det_grad<e>(gD);
 #pragma unroll
-      for (int k = 0; k < n; ++k) lD += (double)ol[e][k] * B[k * ld + i];
+      for (int k = 0; k < n; ++k) lD += (F)ol[e][k] * B[k * ld + i];
       R gJ[3];
       jas_grad<e>(gJ);
       R lJ = ljen[e];
 #pragma unroll
       for (int m = 0; m < N; ++m)
         if (m != e) lJ += pl[pidx(e, m)];
-      double dot = 0.0, gj2 = 0.0;
+      F dot = F(0), gj2 = F(0);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const double gj = (double)gJ[c];
+        const F gj = (F)gJ[c];
         dot += gD[c] * gj;
         gj2 += gj * gj;
-        if (grad) grad[3 * e + c] = gD[c] + gj;
+        if (grad) grad[3 * e + c] = to_d(gD[c] + gj);
       }
-      lap += lD + (double)lJ + 2.0 * dot + gj2;
-      if (sp.pot_kind == 0) V += (double)ven[e];
-      else V += (double)sp.half_omega2 * (x[e][0] * x[e][0] + x[e][1] * x[e][1] + x[e][2] * x[e][2]);
+      lap += lD + (F)lJ + twice(dot) + gj2;
+      if (sp.pot_kind == 0) V += (F)ven[e];
+      else V += (F)sp.half_omega2 * (x[e][0] * x[e][0] + x[e][1] * x[e][1] + x[e][2] * x[e][2]);
       if constexpr (PM > 0) {
 #pragma unroll
         for (int p = 0; p < PM; ++p) {
-          double s = 0.0;
+          F s = F(0);
 #pragma unroll
-          for (int k = 0; k < n; ++k) s += (double)odz[e][k][p] * B[k * ld + i];
+          for (int k = 0; k < n; ++k) s += (F)odz[e][k][p] * B[k * ld + i];
           O[p] += s;
         }
-        djs += (double)djen[e];
+        djs += (F)djen[e];
       }
     });
     if (sp.pot_kind == 0) {
 #pragma unroll
-      for (int p = 0; p < NP; ++p) V += (double)pinv[p];
-      V += sp.vnn;
+      for (int p = 0; p < NP; ++p) V += (F)pinv[p];
+      if constexpr (DF) V += sp.vnn_r;
+      else V += sp.vnn;
     }
     if constexpr (PM > 0) {
-      double dudb = 0.0, dpoly[kMaxPoly] = {0.0, 0.0, 0.0, 0.0};
+      F dudb = F(0), dpoly[kMaxPoly] = {F(0), F(0), F(0), F(0)};
 #pragma unroll
       for (int p = 0; p < NP; ++p) {
-        dudb += (double)pdb[p];
+        dudb += (F)pdb[p];
         // d u / d b_(q+3) = R^(q+2)
-        double rk = (double)prs[p] * (double)prs[p];
+        F rk = (F)prs[p] * (F)prs[p];
+        #pragma unroll 1
         for (int q = 0; q < sp.ee_npoly; ++q) {
           dpoly[q] += rk;
-          rk *= (double)prs[p];
+          rk *= (F)prs[p];
         }
       }
 #pragma unroll
       for (int p = 0; p < PM; ++p) {
-        if (p >= sp.n_exp) O[p] = 0.0;  // slots past the exponents hold Jastrow derivatives
+        if (p >= sp.n_exp) O[p] = F(0);  // slots past the exponents hold Jastrow derivatives
         if (sp.ee_on && p == sp.off_ee) O[p] = dudb;
 #pragma unroll
         for (int q = 0; q < kMaxPoly; ++q)
@@ -805,8 +872,9 @@ struct Walker {
         if (EN && p == sp.off_en) O[p] = djs;
       }
     }
-    if (lapout) *lapout = lap;
-    return -0.5 * lap + V;
+    if (lapout) *lapout = to_d(lap);
+    if constexpr (DF) return V - df_scale(lap, 0.5f);
+    else return -0.5 * lap + V;
   }
 };
 
