@@ -365,8 +365,8 @@ def helium_leg(ctx) -> dict:
     case: Z = 2, psi = exp(-alpha (r1 + r2)) exp(r12 / (2 (1 + beta r12))),
     alpha 1.6875, beta 0.3, 1,024 walkers started N(0, 1) bohr, box moves of
     side 0.5 bohr, 1,000 unsampled + 10,000 sampled sweeps, E_L every sweep,
-    FP64 (and the mixed form beside it); the CPU port runs the same workload
-    on all host threads."""
+    FP64 (and the mixed and FP64-accurate double-float forms beside it); the
+    CPU port runs the same workload on all host threads."""
     import numpy as np
 
     from mole_gb300 import api
@@ -375,7 +375,7 @@ def helium_leg(ctx) -> dict:
 
     W, n_eq, n_steps = 1024, 1000, 10000
     out = {"workload": "He singlet VMC, 1024 walkers, box 0.5 bohr, 1000 + 10000 sweeps", "walkers": W}
-    for name, prec in (("fp64", api.PREC_FP64), ("mixed", api.PREC_MIXED)):
+    for name, prec in (("fp64", api.PREC_FP64), ("mixed", api.PREC_MIXED), ("df64", api.PREC_DF64)):
         wf = api.WaveFunction(ctx, S.helium(1.6875, 0.3))
         wk = api.Walkers(wf, W, seed=0x5EED)
         samp = api.Sampler(wf, api.MetropolisBox(0.5), wk, precision=prec)

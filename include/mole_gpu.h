@@ -166,6 +166,12 @@ int mole_ctx_device_info(mole_ctx* ctx, int32_t* n_sm, int32_t* cc_major, int32_
  * native FP64 because a value left FP32's exponent range (no reference
  * counterpart: the reference computes in f64 only). */
 int mole_ctx_df64_reruns(mole_ctx* ctx, int64_t* reruns);
+/* Evaluates the library's device arithmetic on n host values x (no reference
+ * counterpart; for accuracy tests): fn 0 = the FP64 exponential of the native
+ * FP64 kernels, 1 = double-float exp, 2 = double-float reciprocal square root,
+ * 3 = double-float reciprocal, 4 = double-float x / (1 + x^2). Results go to
+ * the host array y. */
+int mole_math_check(mole_ctx* ctx, int32_t fn, const double* x, int64_t n, double* y);
 /* Device FP64 and FP32 FMA peaks measured by a microbenchmark (GFLOP/s). */
 int mole_probe_peaks(mole_ctx* ctx, double* fp64_gflops, double* fp32_gflops);
 

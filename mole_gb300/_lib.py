@@ -70,6 +70,7 @@ SIGNATURES = {
     "mole_ctx_kernel_time": (C.c_int, [_P, C.c_int32, _D, C.POINTER(C.c_int64)]),
     "mole_probe_peaks": (C.c_int, [_P, _D, _D]),
     "mole_ctx_df64_reruns": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "mole_math_check": (C.c_int, [_P, C.c_int32, _D, C.c_int64, _D]),
     "mole_ctx_device_info": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "mole_system_create": (C.c_int, [_P, C.POINTER(SystemDesc), _D, C.c_int32, C.POINTER(_P)]),
     "mole_system_destroy": (C.c_int, [_P]),

@@ -83,6 +83,14 @@ class Context:
         check(self.lib.mole_ctx_df64_reruns(self.h, C.byref(n)))
         return n.value
 
+    def math_check(self, fn: int, x) -> np.ndarray:
+        """The library's device arithmetic on x (0: FP64 exp of the native kernels,
+        1-4: double-float exp, rsqrt, reciprocal, x / (1 + x^2))."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty_like(x)
+        check(self.lib.mole_math_check(self.h, fn, dptr(x), x.size, dptr(y)))
+        return y
+
     def probe_peaks(self) -> tuple[float, float]:
         """(FP64, FP32) FMA GFLOP/s measured on this device."""
         a, b = C.c_double(), C.c_double()

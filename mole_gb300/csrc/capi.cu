@@ -331,6 +331,19 @@ int mole_ctx_kernel_time(mole_ctx* c, int32_t kernel, double* total_ms, int64_t*
   return MOLE_OK;
 }
 
+int mole_math_check(mole_ctx* c, int32_t fn, const double* x, int64_t n, double* y) {
+  cudaGetLastError();
+  if (!c || !x || !y || n < 0 || fn < 0 || fn > 4) return fail(MOLE_ERR_INVALID_ARG, "bad argument");
+  CUDA_TRY(c->scratch.reserve((size_t)2 * std::max<int64_t>(n, 1)));
+  double* dx = c->scratch.p;
+  double* dy = dx + n;
+  CUDA_TRY(cudaMemcpyAsync(dx, x, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(launch_math_check(fn, dx, n, dy, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(y, dy, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return MOLE_OK;
+}
+
 int mole_ctx_df64_reruns(mole_ctx* c, int64_t* reruns) {
   if (!c || !reruns) return fail(MOLE_ERR_INVALID_ARG, "NULL argument");
   *reruns = c->df64_reruns;

@@ -20,6 +20,13 @@
 //                 2^(j/64), degree-5 polynomial on |r| <= ln2/128
 // Every FP32 operation in the transformations uses the _rn intrinsics so that
 // the compiler cannot contract or reassociate them.
+//
+// exp64 is an FP64 exponential for the native FP64 kernels built on the same
+// pieces: FP64 argument reduction, e^r - 1 in double-float (small enough that
+// 2^-47 relative is below half an FP64 ulp of the result), one FP64 FMA to
+// finish. Five FP64-pipe instructions instead of the library's fifteen
+// (measured with the FP64-pipe instruction counter); float <-> double
+// conversions do not use the FP64 pipe.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -136,16 +143,64 @@ __device__ __forceinline__ df64 df_rsqrt(df64 a) {
 }
 __device__ __forceinline__ df64 df_sqrt(df64 a) { return a.h > 0.f ? a * df_rsqrt(a) : df64(0.f, 0.f); }
 
-// 2^(j/64), j = 0..63, as df64 pairs in the CTA's shared memory; every kernel
-// that evaluates df_exp calls df64_setup() with all its threads first.
-static __shared__ float2 g_df64_exp2_tab[64];
-__device__ __forceinline__ void df64_setup() {
-  for (int j = threadIdx.x; j < 64; j += blockDim.x) {
-    const double v = exp2((double)j / 64.0);
-    const float h = (float)v;
-    g_df64_exp2_tab[j] = make_float2(h, (float)(v - (double)h));
-  }
-  __syncthreads();
+// 2^(j/64), j = 0..63, rounded to FP64 (read through the L1 cache: a warp's
+// lanes touch at most 64 distinct 8-byte entries, 4 cache lines).
+static __device__ __align__(16) const double kExp2Tab64[64] = {
+    0x1.0000000000000p+0, 0x1.02c9a3e778061p+0, 0x1.059b0d3158574p+0, 0x1.0874518759bc8p+0,
+    0x1.0b5586cf9890fp+0, 0x1.0e3ec32d3d1a2p+0, 0x1.11301d0125b51p+0, 0x1.1429aaea92de0p+0,
+    0x1.172b83c7d517bp+0, 0x1.1a35beb6fcb75p+0, 0x1.1d4873168b9aap+0, 0x1.2063b88628cd6p+0,
+    0x1.2387a6e756238p+0, 0x1.26b4565e27cddp+0, 0x1.29e9df51fdee1p+0, 0x1.2d285a6e4030bp+0,
+    0x1.306fe0a31b715p+0, 0x1.33c08b26416ffp+0, 0x1.371a7373aa9cbp+0, 0x1.3a7db34e59ff7p+0,
+    0x1.3dea64c123422p+0, 0x1.4160a21f72e2ap+0, 0x1.44e086061892dp+0, 0x1.486a2b5c13cd0p+0,
+    0x1.4bfdad5362a27p+0, 0x1.4f9b2769d2ca7p+0, 0x1.5342b569d4f82p+0, 0x1.56f4736b527dap+0,
+    0x1.5ab07dd485429p+0, 0x1.5e76f15ad2148p+0, 0x1.6247eb03a5585p+0, 0x1.6623882552225p+0,
+    0x1.6a09e667f3bcdp+0, 0x1.6dfb23c651a2fp+0, 0x1.71f75e8ec5f74p+0, 0x1.75feb564267c9p+0,
+    0x1.7a11473eb0187p+0, 0x1.7e2f336cf4e62p+0, 0x1.82589994cce13p+0, 0x1.868d99b4492edp+0,
+    0x1.8ace5422aa0dbp+0, 0x1.8f1ae99157736p+0, 0x1.93737b0cdc5e5p+0, 0x1.97d829fde4e50p+0,
+    0x1.9c49182a3f090p+0, 0x1.a0c667b5de565p+0, 0x1.a5503b23e255dp+0, 0x1.a9e6b5579fdbfp+0,
+    0x1.ae89f995ad3adp+0, 0x1.b33a2b84f15fbp+0, 0x1.b7f76f2fb5e47p+0, 0x1.bcc1e904bc1d2p+0,
+    0x1.c199bdd85529cp+0, 0x1.c67f12e57d14bp+0, 0x1.cb720dcef9069p+0, 0x1.d072d4a07897cp+0,
+    0x1.d5818dcfba487p+0, 0x1.da9e603db3285p+0, 0x1.dfc97337b9b5fp+0, 0x1.e502ee78b3ff6p+0,
+    0x1.ea4afa2a490dap+0, 0x1.efa1bee615a27p+0, 0x1.f50765b6e4540p+0, 0x1.fa7c1819e90d8p+0,
+};
+// The same values as double-float pairs.
+static __device__ __align__(16) const float kExp2TabDF[64][2] = {
+    {0x1.0000000000000p+0f, 0x0.0p+0f}, {0x1.02c9a40000000p+0f, -0x1.887fa00000000p-28f},
+    {0x1.059b0e0000000p+0f, -0x1.9d4f520000000p-25f}, {0x1.0874520000000p+0f, -0x1.e2990e0000000p-26f},
+    {0x1.0b55860000000p+0f, 0x1.9f31220000000p-25f}, {0x1.0e3ec40000000p+0f, -0x1.a585cc0000000p-25f},
+    {0x1.11301e0000000p+0f, -0x1.fdb4960000000p-25f}, {0x1.1429aa0000000p+0f, 0x1.d525bc0000000p-25f},
+    {0x1.172b840000000p+0f, -0x1.c157420000000p-27f}, {0x1.1a35be0000000p+0f, 0x1.6df96e0000000p-25f},
+    {0x1.1d48740000000p+0f, -0x1.d2e8ca0000000p-25f}, {0x1.2063b80000000p+0f, 0x1.0c519a0000000p-25f},
+    {0x1.2387a60000000p+0f, 0x1.ceac480000000p-25f}, {0x1.26b4560000000p+0f, 0x1.789f380000000p-26f},
+    {0x1.29e9e00000000p+0f, -0x1.5c04240000000p-25f}, {0x1.2d285a0000000p+0f, 0x1.b900c20000000p-26f},
+    {0x1.306fe00000000p+0f, 0x1.4636e20000000p-25f}, {0x1.33c08c0000000p+0f, -0x1.b37d200000000p-25f},
+    {0x1.371a740000000p+0f, -0x1.18aac60000000p-25f}, {0x1.3a7db40000000p+0f, -0x1.634c020000000p-25f},
+    {0x1.3dea640000000p+0f, 0x1.8246840000000p-25f}, {0x1.4160a20000000p+0f, 0x1.f72e2a0000000p-28f},
+    {0x1.44e0860000000p+0f, 0x1.8624b40000000p-30f}, {0x1.486a2c0000000p+0f, -0x1.47d8660000000p-25f},
+    {0x1.4bfdae0000000p+0f, -0x1.593abc0000000p-25f}, {0x1.4f9b280000000p+0f, -0x1.2c5a6c0000000p-25f},
+    {0x1.5342b60000000p+0f, -0x1.2c56100000000p-25f}, {0x1.56f4740000000p+0f, -0x1.295b040000000p-25f},
+    {0x1.5ab07e0000000p+0f, -0x1.5bd5ec0000000p-27f}, {0x1.5e76f20000000p+0f, -0x1.4a5bd60000000p-25f},
+    {0x1.6247ec0000000p+0f, -0x1.f8b5500000000p-25f}, {0x1.6623880000000p+0f, 0x1.2a91120000000p-27f},
+    {0x1.6a09e60000000p+0f, 0x1.9fcef40000000p-26f}, {0x1.6dfb240000000p+0f, -0x1.cd72e80000000p-27f},
+    {0x1.71f75e0000000p+0f, 0x1.1d8bee0000000p-25f}, {0x1.75feb60000000p+0f, -0x1.37b3060000000p-25f},
+    {0x1.7a11480000000p+0f, -0x1.829fd00000000p-25f}, {0x1.7e2f340000000p+0f, -0x1.2616340000000p-25f},
+    {0x1.82589a0000000p+0f, -0x1.accc7c0000000p-26f}, {0x1.868d9a0000000p+0f, -0x1.2edb440000000p-26f},
+    {0x1.8ace540000000p+0f, 0x1.15506e0000000p-27f}, {0x1.8f1aea0000000p+0f, -0x1.baa2320000000p-26f},
+    {0x1.93737c0000000p+0f, -0x1.e647440000000p-25f}, {0x1.97d82a0000000p+0f, -0x1.0d8d840000000p-31f},
+    {0x1.9c49180000000p+0f, 0x1.51f8480000000p-27f}, {0x1.a0c6680000000p+0f, -0x1.2886a60000000p-26f},
+    {0x1.a5503c0000000p+0f, -0x1.b83b540000000p-25f}, {0x1.a9e6b60000000p+0f, -0x1.50c0480000000p-25f},
+    {0x1.ae89fa0000000p+0f, -0x1.a94b140000000p-26f}, {0x1.b33a2c0000000p+0f, -0x1.ec3a820000000p-26f},
+    {0x1.b7f7700000000p+0f, -0x1.a094380000000p-25f}, {0x1.bcc1ea0000000p+0f, -0x1.f687c60000000p-25f},
+    {0x1.c199be0000000p+0f, -0x1.3d56b20000000p-27f}, {0x1.c67f120000000p+0f, 0x1.cafa2a0000000p-25f},
+    {0x1.cb720e0000000p+0f, -0x1.8837cc0000000p-27f}, {0x1.d072d40000000p+0f, 0x1.40f1300000000p-25f},
+    {0x1.d5818e0000000p+0f, -0x1.822dbc0000000p-27f}, {0x1.da9e600000000p+0f, 0x1.ed99420000000p-27f},
+    {0x1.dfc9740000000p+0f, -0x1.908c940000000p-25f}, {0x1.e502ee0000000p+0f, 0x1.e2cffe0000000p-26f},
+    {0x1.ea4afa0000000p+0f, 0x1.52486c0000000p-27f}, {0x1.efa1be0000000p+0f, 0x1.cc2b440000000p-25f},
+    {0x1.f507660000000p+0f, -0x1.246eb00000000p-26f}, {0x1.fa7c180000000p+0f, 0x1.9e90d80000000p-28f},
+};
+__device__ __forceinline__ df64 df_exp2_tab(int j) {
+  const float2 v = __ldg(reinterpret_cast<const float2*>(kExp2TabDF[j]));
+  return df64(v.x, v.y);
 }
 
 // e^x. x = n ln2/64 + r with n = rint(64 x / ln2) (|n| < 2^13, so n L1 is
@@ -165,8 +220,10 @@ __device__ __forceinline__ df64 df_exp(df64 x) {
   const float t = __fmaf_rn(-n, kL1, x.h);  // exact
   const float p2 = __fmul_rn(n, kL2);
   const float e2 = __fmaf_rn(n, kL2, -p2);
+  // r = t - n L2 - n L3 + x.l: the two large parts exactly, the small ones in FP32
   const df64 a = df_two_sum(t, -p2);
-  const df64 r = df_two_sum(a.h, __fadd_rn(a.l, __fsub_rn(__fsub_rn(x.l, e2), __fmul_rn(n, kL3))));
+  const df64 b = df_two_sum(a.h, x.l);
+  const df64 r = df_fast_two_sum(b.h, __fsub_rn(__fsub_rn(__fadd_rn(a.l, b.l), e2), __fmul_rn(n, kL3)));
   // r^2 / 2 in double-float, the cubic tail in FP32
   const float s = __fmul_rn(r.h, r.h);
   const float se = __fmaf_rn(__fadd_rn(r.h, r.h), r.l, __fmaf_rn(r.h, r.h, -s));
@@ -178,12 +235,40 @@ __device__ __forceinline__ df64 df_exp(df64 x) {
   const df64 eq = df_two_sum(E.h, q);
   E = df_fast_two_sum(eq.h, __fadd_rn(eq.l, E.l));
   const int ni = (int)n;
-  const float2 tb = g_df64_exp2_tab[ni & 63];
-  const df64 T(tb.x, tb.y);
+  const df64 T = df_exp2_tab(ni & 63);
   const df64 v = T + T * E;
   const int k = ni >> 6;  // floor division
   if (k < -126) return df64(0.f, 0.f);
   return df_scale(v, __int_as_float((k + 127) << 23));
+}
+
+// e^x in FP64 to about 1.5 ulp. x = n ln2/64 + r, n = rint(64 x / ln2) from the
+// FP32 value of x, r = x - n L1 - n L2 in FP64 (L1: 37-bit head of ln2/64, so
+// n L1 is exact for |n| < 2^16); q = e^r - 1 = r + r^2/2 + r^3/6 in
+// double-float plus r^4/24 + r^5/120 + r^6/720 in FP32 (|q| < 0.0056, error
+// below 2^-54); e^x = 2^(n >> 6) (T + T q), T = 2^((n & 63)/64). Outside
+// |x| < 700 (overflow, subnormal results) the library exp.
+__device__ __forceinline__ double exp64(double x) {
+  const float xf = __double2float_rn(x);
+  if (!(fabsf(xf) < 700.f)) return exp(x);
+  constexpr double kL1 = 0x1.62e42fefa0000p-7;
+  constexpr double kL2 = 0x1.cf79abc9e3b3ap-46;
+  const float n = rintf(__fmul_rn(xf, 92.33248261689366f));
+  const double nd = (double)n;
+  double r = fma(-nd, kL1, x);
+  r = fma(-nd, kL2, r);
+  const float rh = __double2float_rn(r);
+  const df64 rd(rh, __double2float_rn(r - (double)rh));
+  float t = __fmaf_rn(rh, 1.0f / 720.0f, 1.0f / 120.0f);
+  t = __fmaf_rn(rh, t, 1.0f / 24.0f);
+  const df64 a = df_mul(rd, t) + df64(0x1.555556p-3f, -0x1.555556p-28f);  // 1/6 + r t
+  const df64 b = rd * a + df64(0.5f);
+  const df64 q = rd + rd * (rd * b);
+  const int ni = (int)n;
+  const double T = __ldg(&kExp2Tab64[ni & 63]);
+  const double v = fma(T, (double)q.h + (double)q.l, T);
+  // scale by 2^(n >> 6) in the exponent field (v is in [1, 2.1), the result normal)
+  return __hiloint2double(__double2hiint(v) + (ni >> 6) * (1 << 20), __double2loint(v));
 }
 
 __device__ __forceinline__ df64& operator+=(df64& a, df64 b) { return a = a + b; }

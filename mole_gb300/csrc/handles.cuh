@@ -37,6 +37,8 @@ struct DevBuf {
   }
 };
 
+cudaError_t launch_math_check(int fn, const double* x, int64_t n, double* y, cudaStream_t s);
+
 // Kernel timing slots of a context (mole_ctx_kernel_time).
 enum { kTimeVmc = 0, kTimeDmc = 1, kTimeEval = 2, kTimeSGemm = 3, kTimeBatch = 4, kTimeSlots = 5 };
 

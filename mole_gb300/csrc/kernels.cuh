@@ -79,7 +79,6 @@ __device__ __forceinline__ void vmc_body(const SysParams<R>& sp, const VmcArgs& 
   const int w = blockIdx.x * a.wpc + threadIdx.x;
   const int tid = threadIdx.x;
   const bool active = tid < a.wpc && w < a.W;
-  if constexpr (Wk::DF) df64_setup();
   F* srf = reinterpret_cast<F*>(srs);  // df64 is 8 bytes like the double slots
   Wk wk;
   wk.nn = nn_setup<R, NN>(sp);
@@ -185,7 +184,6 @@ template <int NU, int ND, class R, int PM, bool EN, bool NN = false>
 __global__ void __launch_bounds__(kBlock) eval_kernel(const __grid_constant__ SysParams<R> sp, const EvalArgs a) {
   using Wk = Walker<NU, ND, R, PM, EN, NN>;
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
-  if constexpr (Wk::DF) df64_setup();
   Wk wk;
   wk.nn = nn_setup<R, NN>(sp);
   if (w >= a.W) return;

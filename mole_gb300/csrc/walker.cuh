@@ -71,7 +71,7 @@ template <class R>
 __device__ __forceinline__ R exp_t(R x);
 template <>
 __device__ __forceinline__ double exp_t<double>(double x) {
-  return exp(x);
+  return exp64(x);
 }
 template <>
 __device__ __forceinline__ float exp_t<float>(float x) {
