@@ -19,9 +19,35 @@ struct KernelSetT {
   Dmc dmc[2];               // [e-n Jastrow]; NULL where not compiled
 };
 
+// Dynamic shared memory that keeps at most `ctas` CTAs of `kernel` resident
+// per SM. The VMC grid is whole waves of (SMs x ctas); a kernel whose
+// registers would admit one CTA more per SM can otherwise be placed unevenly
+// (some SMs holding ctas + 1 CTAs, others fewer), stretching the launch by
+// up to (ctas + 1) / ctas. Computed once per kernel on the current device.
+template <class K>
+size_t residency_pad(K kernel, int ctas, cudaError_t* err) {
+  int dev = 0, per_sm = 0, reserved = 0;
+  cudaFuncAttributes fa;
+  if ((*err = cudaGetDevice(&dev)) != cudaSuccess) return 0;
+  if ((*err = cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess) return 0;
+  if ((*err = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev)) != cudaSuccess) return 0;
+  if ((*err = cudaFuncGetAttributes(&fa, kernel)) != cudaSuccess) return 0;
+  const long need = per_sm / (ctas + 1) + 1 - reserved - (long)fa.sharedSizeBytes;  // ctas + 1 do not fit
+  if (need <= 0) return 0;
+  if ((long)ctas * (need + reserved + (long)fa.sharedSizeBytes) > per_sm) return 0;  // keep ctas resident
+  if (need > 48 * 1024 &&
+      (*err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need)) != cudaSuccess)
+    return 0;
+  return (size_t)need;
+}
+
 template <int NU, int ND, class R, int PM, bool DRIFT, bool EN>
 cudaError_t launch_vmc(const SysParams<R>& sp, const VmcArgs& a, int grid, cudaStream_t s) {
-  vmc_kernel<NU, ND, R, PM, DRIFT, EN><<<grid, kBlock, 0, s>>>(sp, a);
+  auto k = vmc_kernel<NU, ND, R, PM, DRIFT, EN>;
+  static cudaError_t pad_err = cudaSuccess;
+  static const size_t pad = residency_pad(k, min_blocks<NU, ND>(), &pad_err);
+  if (pad_err != cudaSuccess) return pad_err;
+  k<<<grid, kBlock, pad, s>>>(sp, a);
   return cudaGetLastError();
 }
 template <int NU, int ND, class R, bool EN>
