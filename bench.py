@@ -407,7 +407,8 @@ def dmc_leg(ctx, n_eq: int = 2000, n_steps: int = 800, train_iters: int = 20) ->
     """DMC on the Be atom (Z = 4, 2 up + 2 down, 1s/2s STO determinant):
     131,072 walkers, time step 0.005, drift-diffusion moves with Metropolis
     accept/reject, a stochastic comb every step, FP64 weights and energy
-    sums with FP32 drift (the mixed form) and the FP64 form beside it.
+    sums with FP32 drift (the mixed form), and the FP64 and FP64-accurate
+    double-float forms beside it.
     Guides: the Pade-Jastrow fallback, and the pair-network Jastrow trained on
     Be by VMC + SR (the LiH recipe). Energies are the mean of the per-step
     ensemble energies after n_eq steps; the error is the larger of the
@@ -458,6 +459,10 @@ def dmc_leg(ctx, n_eq: int = 2000, n_steps: int = 800, train_iters: int = 20) ->
     m, f = out["pade_mixed"], out["pade_fp64"]
     out["pade_mixed"]["energy_delta_vs_fp64"] = m["energy"] - f["energy"]
     out["pade_mixed"]["delta_sigma"] = float(np.hypot(m["error"], f["error"]))
+    r0 = ctx.df64_reruns()
+    out["pade_df64"] = run(pade, api.PREC_DF64, n_steps, "pade_df64")
+    out["pade_df64"]["fp64_reruns"] = ctx.df64_reruns() - r0
+    out["pade_df64"]["energy_delta_vs_fp64"] = out["pade_df64"]["energy"] - f["energy"]
     # neural guide: pair networks trained on Be by VMC + SR from Gaussian(0, 0.01^2) weights
     s = S.beryllium(neural=True, rng=np.random.default_rng(5))
     wf = api.WaveFunction(ctx, s)

@@ -60,10 +60,11 @@ enum { MOLE_MOVE_BOX = 0, MOLE_MOVE_GAUSS = 1, MOLE_MOVE_DIFFUSE = 2 };
  * Sherman-Morrison ratio products, E_L and accumulation, or FP64-accurate
  * double-float: every term as a pair of FP32 numbers (48 significant bits) on
  * the FP32 pipe, results within about 1e-13 relative of FP64. MOLE_PREC_DF64
- * applies to box and Gaussian VMC sweeps and to mole_eval of the fixed-size
- * families (SR sums of at most 2 parameters); a launch whose values leave
- * FP32's exponent range is rerun in native FP64 on the device, and every other
- * call treats MOLE_PREC_DF64 as MOLE_PREC_FP64 */
+ * applies to box and Gaussian VMC sweeps (SR sums of at most 2 parameters),
+ * mole_eval and mole_dmc_run of the non-neural fixed-size families; a call
+ * whose values leave FP32's exponent range (or, in DMC, whose walkers meet a
+ * node) is rerun in native FP64 on the device, and every other call treats
+ * MOLE_PREC_DF64 as MOLE_PREC_FP64 */
 enum { MOLE_PREC_FP64 = 0, MOLE_PREC_MIXED = 1, MOLE_PREC_DF64 = 2 };
 /* initial positions: N(0, width^2) per coordinate, or U(-width, width) as
  * Sampler::new does (src/montecarlo/src/samplers.rs:44-55) */

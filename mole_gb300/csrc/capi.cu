@@ -23,6 +23,8 @@ MOLE_DECL(2, 2)
   DfParts df_parts_vmc_##NU##_##ND##_1();         \
   DfParts df_parts_eval_##NU##_##ND##_0();        \
   DfParts df_parts_eval_##NU##_##ND##_1();        \
+  DfParts df_parts_dmc_##NU##_##ND##_0();         \
+  DfParts df_parts_dmc_##NU##_##ND##_1();         \
   const KernelSetT<df64>* kernels_df_##NU##_##ND() { \
     static const KernelSetT<df64> ks = [] {       \
       KernelSetT<df64> k{};                       \
@@ -33,6 +35,8 @@ MOLE_DECL(2, 2)
       }                                           \
       k.eval[0] = df_parts_eval_##NU##_##ND##_0().eval; \
       k.eval[1] = df_parts_eval_##NU##_##ND##_1().eval; \
+      k.dmc[0] = df_parts_dmc_##NU##_##ND##_0().dmc; \
+      k.dmc[1] = df_parts_dmc_##NU##_##ND##_1().dmc; \
       return k;                                   \
     }();                                          \
     return &ks;                                   \
@@ -1157,11 +1161,15 @@ int mole_dmc_run(mole_walkers* w, const mole_dmc_opts* o, double* energies, doub
     CUDA_TRY(cudaMemsetAsync(c->status.p, 0, sizeof(int), c->stream));
     w->eloc_valid = true;
   }
-  const uint64_t step = w->step;
-  CombState cs0 = {0.0, 0.0, 0.0, 0.0, 0.0};
-  CUDA_TRY(cudaMemcpyAsync(w->dstep, &step, sizeof(uint64_t), cudaMemcpyHostToDevice, c->stream));
-  CUDA_TRY(cudaMemcpyAsync(w->e_ref, &o->e_ref, sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  CUDA_TRY(cudaMemcpyAsync(w->comb, &cs0, sizeof(CombState), cudaMemcpyHostToDevice, c->stream));
+  // the double-float steps keep the starting positions and E_L for a native rerun
+  auto ddf = o->precision == MOLE_PREC_DF64 && !s->nn_on && s->kdf ? s->kdf->dmc[s->en_on] : nullptr;
+  const size_t pos_n = (size_t)NC * W;
+  if (ddf) {
+    CUDA_TRY(c->pos_backup.reserve(pos_n + W));
+    CUDA_TRY(cudaMemcpyAsync(c->pos_backup.p, w->pos, sizeof(double) * pos_n, cudaMemcpyDeviceToDevice, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(c->pos_backup.p + pos_n, w->eloc, sizeof(double) * W, cudaMemcpyDeviceToDevice,
+                             c->stream));
+  }
   DmcArgs a;
   a.W = W;
   a.tau = o->tau;
@@ -1172,16 +1180,42 @@ int mole_dmc_run(mole_walkers* w, const mole_dmc_opts* o, double* energies, doub
   a.partials = c->partials.p;
   a.status = c->status.p;
   a.weight = w->weight;
+  // n_steps steps of one kernel variant from the state at the call's start
+  auto run_steps = [&](auto kernel, const auto& sp) -> int {
+    const uint64_t step = w->step;
+    CombState cs0 = {0.0, 0.0, 0.0, 0.0, 0.0};
+    CUDA_TRY(cudaMemcpyAsync(w->dstep, &step, sizeof(uint64_t), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(w->e_ref, &o->e_ref, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(w->comb, &cs0, sizeof(CombState), cudaMemcpyHostToDevice, c->stream));
+    for (int t = 0; t < o->n_steps; ++t) {
+      a.pos = w->pos;
+      a.eloc = w->eloc;
+      CUDA_TRY(kernel(sp, a, grid, c->stream));
+      CUDA_TRY(launch_comb(w->weight, w->cum, w->btot, nb, c->partials.p, grid, w->comb, w->dstep, w->seed,
+                           w->energies, t, w->pos, w->eloc, w->pos2, w->eloc2, W, NC, c->stream));
+      std::swap(w->pos, w->pos2);
+      std::swap(w->eloc, w->eloc2);
+    }
+    return MOLE_OK;
+  };
   Timer tm(c, 1);
-  for (int t = 0; t < o->n_steps; ++t) {
-    a.pos = w->pos;
-    a.eloc = w->eloc;
-    if (mixed) CUDA_TRY(dmc32(s)(s->sp32, a, grid, c->stream));
-    else CUDA_TRY(dmc64(s)(s->sp64, a, grid, c->stream));
-    CUDA_TRY(launch_comb(w->weight, w->cum, w->btot, nb, c->partials.p, grid, w->comb, w->dstep, w->seed,
-                         w->energies, t, w->pos, w->eloc, w->pos2, w->eloc2, W, NC, c->stream));
-    std::swap(w->pos, w->pos2);
-    std::swap(w->eloc, w->eloc2);
+  if (ddf) rc = run_steps(ddf, s->spdf);
+  else if (mixed) rc = run_steps(dmc32(s), s->sp32);
+  else rc = run_steps(dmc64(s), s->sp64);
+  if (rc) return rc;
+  if (ddf) {
+    int st = 0;
+    CUDA_TRY(cudaMemcpyAsync(&st, c->status.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (st & 8) {
+      // a walker left FP32's range or met a node: the same steps in native FP64
+      ++c->df64_reruns;
+      CUDA_TRY(cudaMemcpyAsync(w->pos, c->pos_backup.p, sizeof(double) * pos_n, cudaMemcpyDeviceToDevice, c->stream));
+      CUDA_TRY(cudaMemcpyAsync(w->eloc, c->pos_backup.p + pos_n, sizeof(double) * W, cudaMemcpyDeviceToDevice,
+                               c->stream));
+      CUDA_TRY(cudaMemsetAsync(c->status.p, 0, sizeof(int), c->stream));
+      if ((rc = run_steps(dmc64(s), s->sp64))) return rc;
+    }
   }
   tm.stop();
   CombState cs;

@@ -295,6 +295,8 @@ __device__ __forceinline__ float mag(df64 x) { return fabsf(x.h); }
 __device__ __forceinline__ bool is_neg(double x) { return x < 0.0; }
 __device__ __forceinline__ bool is_neg(df64 x) { return x.h < 0.f; }
 __device__ __forceinline__ bool is_zero(double x) { return x == 0.0; }
+__device__ __forceinline__ bool is_pos(double x) { return x > 0.0; }
+__device__ __forceinline__ bool is_pos(df64 x) { return x.h > 0.f; }
 __device__ __forceinline__ bool is_zero(df64 x) { return x.h == 0.f; }
 __device__ __forceinline__ double recip(double x) { return 1.0 / x; }
 __device__ __forceinline__ df64 recip(df64 x) { return df_rcp(x); }

@@ -94,15 +94,19 @@ typename KernelSetT<R>::Dmc maybe_dmc() {
 struct DfParts {
   KernelSetT<df64>::Vmc vmc[kPmSlots];  // [PM slot]; slot 2 (eight-wide SR) not compiled
   KernelSetT<df64>::Eval eval;
+  KernelSetT<df64>::Dmc dmc;
 };
 #define MOLE_INSTANTIATE_DF_VMC(NU, ND, EN)                                                   \
   DfParts df_parts_vmc_##NU##_##ND##_##EN() {                                                \
     return DfParts{{launch_vmc<NU, ND, df64, 0, false, EN>, launch_vmc<NU, ND, df64, 2, false, EN>, nullptr}, \
-                   nullptr};                                                                 \
+                   nullptr, nullptr};                                                        \
   }
 #define MOLE_INSTANTIATE_DF_EVAL(NU, ND)                                                      \
-  DfParts df_parts_eval_##NU##_##ND##_0() { return DfParts{{}, launch_eval<NU, ND, df64, false>}; } \
-  DfParts df_parts_eval_##NU##_##ND##_1() { return DfParts{{}, launch_eval<NU, ND, df64, true>}; }
+  DfParts df_parts_eval_##NU##_##ND##_0() { return DfParts{{}, launch_eval<NU, ND, df64, false>, nullptr}; } \
+  DfParts df_parts_eval_##NU##_##ND##_1() { return DfParts{{}, launch_eval<NU, ND, df64, true>, nullptr}; }
+#define MOLE_INSTANTIATE_DF_DMC(NU, ND)                                                       \
+  DfParts df_parts_dmc_##NU##_##ND##_0() { return DfParts{{}, nullptr, launch_dmc<NU, ND, df64, false>}; } \
+  DfParts df_parts_dmc_##NU##_##ND##_1() { return DfParts{{}, nullptr, launch_dmc<NU, ND, df64, true>}; }
 
 const KernelSetT<double>* kernel_set64(int nu, int nd);
 const KernelSetT<float>* kernel_set32(int nu, int nd);

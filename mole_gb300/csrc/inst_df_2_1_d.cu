@@ -1,0 +1,6 @@
+// Double-float (FP64-accurate) DMC step launchers, spin blocks of 2 up and 1 down electrons.
+#include "dispatch.cuh"
+
+namespace mole {
+MOLE_INSTANTIATE_DF_DMC(2, 1)
+}  // namespace mole

@@ -239,7 +239,11 @@ __global__ void __launch_bounds__(kBlock, (min_blocks<NU, ND>())) dmc_step_kerne
     wk.load(a.pos, a.W, w);
     const double e_old = a.eloc[w];
     v[2] = (double)Wk::N;
-    if (!wk.refresh(sp, nullptr, nullptr)) {
+    const bool regular = wk.refresh(sp, nullptr, nullptr);
+    // the df64 form cannot tell a node from FP32 range loss: the host reruns
+    // the steps in native FP64, which decides
+    if (Wk::DF && (!regular || wk.oor)) atomicOr(a.status, 8);
+    if (!regular) {
       // an exactly singular Slater matrix: psi = 0 at the precision of the
       // orbital values (the walker sits on a node, or an electron is so far
       // out that every orbital underflows), so the walker carries no weight,
@@ -250,8 +254,9 @@ __global__ void __launch_bounds__(kBlock, (min_blocks<NU, ND>())) dmc_step_kerne
       v[0] = e_old;
       if (!(e_old == e_old)) atomicOr(a.status, 1);
       const int nacc = wk.template sweep<kMoveDiffuse>(sp, (R)a.tau, a.seed, (uint32_t)w, t);
-      double O[1];
-      const double e_new = wk.local_energy(sp, O, nullptr, nullptr);
+      typename Wk::F O[1];
+      const double e_new = to_d(wk.local_energy(sp, O, nullptr, nullptr));
+      if (Wk::DF && (wk.oor || !(e_new == e_new))) atomicOr(a.status, 8);
       wk.store(a.pos, a.W, w);
       a.eloc[w] = e_new;
       const double er = *a.e_ref;

@@ -2,6 +2,8 @@
 // and the FP64 CG solve for stochastic reconfiguration with many parameters.
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
 #include "sr_large.cuh"
 
 namespace mole {
@@ -9,117 +11,200 @@ namespace mole {
 // --------------------------------------------------------------- O_k (network)
 
 constexpr int kNnMaxPairs = 8;
+constexpr int kOgenWarps = 8;  // walkers in flight per CTA (one per warp)
+constexpr int kOgenPB = 4;     // pairs per GEMV pass: each weight load feeds kOgenPB FMAs
+constexpr int kW2Ld = kNnH + 1;  // padded row of the transposed W2: conflict-free both ways
 
 struct OgenShared {
-  float W1[2][kNnH][kNnIn];
-  float b1[2][kNnH];
-  float W2[2][kNnH][kNnH];   // [a][c]
-  float W2T[2][kNnH][kNnH];  // [c][a]
-  float b2[2][kNnH];
-  float w3[2][kNnH];
-  float h1[kNnMaxPairs][kNnH];
-  float d2[kNnMaxPairs][kNnH];
-  float x[kMaxElec * 3];  // the walker's positions (FP32: these O_k are FP32 quantities)
+  float W2p[2][kNnH][kW2Ld];                     // W2p[net][c][a] = W2[a][c]
+  float W1[2][kNnH][kNnIn], b1[2][kNnH], b2[2][kNnH], w3[2][kNnH];
+  float d2s[kOgenWarps][kNnMaxPairs][kNnH];      // per warp: delta2 of each pair
 };
 
-// d J_nn / d theta for one walker per CTA iteration; thread a is hidden unit a.
-// J_nn = sum over pairs of y(pair), so each gradient is a sum over pairs;
-// dW2[a][c] = sum_p delta2[p][a] h1[p][c] is written with thread c writing
-// consecutive addresses.
+// d J_nn / d theta of one walker per warp. J_nn = sum over pairs of y(pair),
+// so every gradient is a sum over the walker's pairs (6 e-e, 8 e-n for LiH).
+// Lane l owns hidden units l and l + 32: its first-layer weights, biases and
+// output weights of the current net sit in registers, W2 (transposed, rows padded to 65 floats
+// so that both the forward and the backward GEMV read it without bank
+// conflicts) in shared memory. The pairs of a net go through the two 64 x 64
+// GEMVs kOgenPB at a time, the activations of the other lanes' units arriving
+// by warp shuffles; dJ/dW2[a][c] = sum_p delta2[p][a] h1[p][c] is then formed
+// with h1 in registers and delta2 broadcast from shared memory, and written
+// row by row in 128-byte segments.
 template <class T>
-__global__ void __launch_bounds__(kNnH) nn_ogen_kernel(const __grid_constant__ SysParams<float> sp, const double* pos,
-                                                       int W, int n_up, int N, T* O, int ldO, int col0) {
+__global__ void __launch_bounds__(kOgenWarps * 32, 2) nn_ogen_kernel(const __grid_constant__ SysParams<float> sp,
+                                                                 const double* pos, int W, int n_up, int N, T* O,
+                                                                 int ldO, int col0) {
   extern __shared__ __align__(16) unsigned char ogen_smem[];
   OgenShared& sh = *reinterpret_cast<OgenShared*>(ogen_smem);
-  const int t = threadIdx.x;
-  for (int i = t; i < 2 * kNnNetP; i += kNnH) {
-    const int n = i / kNnNetP, k = i % kNnNetP;
-    const float v = (float)sp.nn_theta[i];
-    if (k < kNnOffB1) sh.W1[n][k / kNnIn][k % kNnIn] = v;
-    else if (k < kNnOffW2) sh.b1[n][k - kNnOffB1] = v;
-    else if (k < kNnOffB2) {
-      const int j = k - kNnOffW2;
-      sh.W2[n][j / kNnH][j % kNnH] = v;
-      sh.W2T[n][j % kNnH][j / kNnH] = v;
-    } else if (k < kNnOffW3) sh.b2[n][k - kNnOffB2] = v;
-    else if (k < kNnOffB3) sh.w3[n][k - kNnOffW3] = v;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < 2 * kNnH * kNnH; i += blockDim.x) {
+    const int n = i / (kNnH * kNnH), j = i % (kNnH * kNnH);
+    sh.W2p[n][j % kNnH][j / kNnH] = (float)sp.nn_theta[n * kNnNetP + kNnOffW2 + j];
+  }
+  for (int i = threadIdx.x; i < 2 * kNnH; i += blockDim.x) {
+    const int n = i / kNnH, u = i % kNnH;
+    const double* th = sp.nn_theta + n * kNnNetP;
+#pragma unroll
+    for (int k = 0; k < kNnIn; ++k) sh.W1[n][u][k] = (float)th[kNnOffW1 + u * kNnIn + k];
+    sh.b1[n][u] = (float)th[kNnOffB1 + u];
+    sh.b2[n][u] = (float)th[kNnOffB2 + u];
+    sh.w3[n][u] = (float)th[kNnOffW3 + u];
   }
   __syncthreads();
-  for (int w = blockIdx.x; w < W; w += gridDim.x) {
-    if (t < 3 * N) sh.x[t] = (float)pos[(size_t)t * W + w];
-    __syncthreads();
+  const int n_warps = gridDim.x * kOgenWarps;
+  for (int w = blockIdx.x * kOgenWarps + warp; w < W; w += n_warps) {
+    // the walker's coordinates, lane t holding coordinate t (FP32: these O_k are FP32 quantities)
+    const float xv = lane < 3 * N ? (float)pos[(size_t)lane * W + w] : 0.f;
     T* out = O + (size_t)w * ldO + col0;
+#pragma unroll 1
     for (int net = 0; net < 2; ++net) {
-      float gW1[kNnIn] = {0.f, 0.f, 0.f, 0.f}, gb1 = 0.f, gb2 = 0.f, gw3 = 0.f;
-      int np = 0;
       const int n_b = net == 0 ? N : sp.n_nuc;
-      for (int i = 0; i < N; ++i)
-        for (int j = (net == 0 ? i + 1 : 0); j < n_b; ++j, ++np) {
-          float d0, d1, d2, s;
+      const int np = net == 0 ? N * (N - 1) / 2 : N * sp.n_nuc;
+      // this lane's units lane and lane + 32 of this net
+      float W1n[2][kNnIn], b1n[2], b2n[2], w3n[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int u = lane + 32 * h;
+#pragma unroll
+        for (int k = 0; k < kNnIn; ++k) W1n[h][k] = sh.W1[net][u][k];
+        b1n[h] = sh.b1[net][u];
+        b2n[h] = sh.b2[net][u];
+        w3n[h] = sh.w3[net][u];
+      }
+      float gW1[2][kNnIn] = {}, gb1[2] = {}, gb2[2] = {}, gw3[2] = {};
+      float h1k[kNnMaxPairs][2];  // h1 of every pair, kept for dJ/dW2
+#pragma unroll
+      for (int p = 0; p < kNnMaxPairs; ++p) h1k[p][0] = h1k[p][1] = 0.f;
+#pragma unroll
+      for (int p0 = 0; p0 < kNnMaxPairs; p0 += kOgenPB) {
+        if (p0 >= np) break;
+        float xf[kOgenPB][kNnIn], h1[kOgenPB][2];
+        bool valid[kOgenPB];
+#pragma unroll
+        for (int q = 0; q < kOgenPB; ++q) {
+          const int p = p0 + q;
+          valid[q] = p < np;
+          // pair p -> (i, j): e-e pairs i < j in order, e-n pairs (electron, nucleus)
+          int i = 0, j = 0;
           if (net == 0) {
-            d0 = sh.x[3 * i] - sh.x[3 * j];
-            d1 = sh.x[3 * i + 1] - sh.x[3 * j + 1];
-            d2 = sh.x[3 * i + 2] - sh.x[3 * j + 2];
+            int rem = valid[q] ? p : 0;
+            while (rem >= N - 1 - i) {
+              rem -= N - 1 - i;
+              ++i;
+            }
+            j = i + 1 + rem;
+          } else {
+            i = valid[q] ? p / n_b : 0;
+            j = valid[q] ? p % n_b : 0;
+          }
+          float d0 = __shfl_sync(0xffffffffu, xv, 3 * i), d1 = __shfl_sync(0xffffffffu, xv, 3 * i + 1),
+                d2 = __shfl_sync(0xffffffffu, xv, 3 * i + 2), s;
+          if (net == 0) {
+            d0 -= __shfl_sync(0xffffffffu, xv, 3 * j);
+            d1 -= __shfl_sync(0xffffffffu, xv, 3 * j + 1);
+            d2 -= __shfl_sync(0xffffffffu, xv, 3 * j + 2);
             s = ((i < n_up) == (j < n_up)) ? 1.f : 0.f;
           } else {
-            d0 = sh.x[3 * i] - sp.nuc_pos[3 * j];
-            d1 = sh.x[3 * i + 1] - sp.nuc_pos[3 * j + 1];
-            d2 = sh.x[3 * i + 2] - sp.nuc_pos[3 * j + 2];
+            d0 -= sp.nuc_pos[3 * j];
+            d1 -= sp.nuc_pos[3 * j + 1];
+            d2 -= sp.nuc_pos[3 * j + 2];
             s = sp.nuc_z[j];
           }
           const float r = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
           const float er = expf(-r);
-          const float x[kNnIn] = {r, er, s * r, s * er};
-          // layer 1 (thread a = unit a)
-          float z = sh.b1[net][t];
+          xf[q][0] = r;
+          xf[q][1] = er;
+          xf[q][2] = s * r;
+          xf[q][3] = s * er;
 #pragma unroll
-          for (int k = 0; k < kNnIn; ++k) z += sh.W1[net][t][k] * x[k];
-          const float h1 = tanhf(z);
-          sh.h1[np][t] = h1;
-          __syncthreads();
-          // layer 2 and output weight (four independent partial sums)
-          float q[4] = {sh.b2[net][t], 0.f, 0.f, 0.f};
-#pragma unroll 4
-          for (int c = 0; c < kNnH; c += 4)
+          for (int h = 0; h < 2; ++h) {
+            float z = b1n[h];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) q[u] += sh.W2T[net][c + u][t] * sh.h1[np][c + u];
-          const float a2 = (q[0] + q[1]) + (q[2] + q[3]);
-          const float h2 = tanhf(a2);
-          const float dl2 = sh.w3[net][t] * (1.f - h2 * h2);
-          sh.d2[np][t] = dl2;
-          gb2 += dl2;
-          gw3 += h2;
-          __syncthreads();
-          // back to layer 1 (thread c = unit c)
-          float r4[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll 4
-          for (int a = 0; a < kNnH; a += 4)
-#pragma unroll
-            for (int u = 0; u < 4; ++u) r4[u] += sh.W2[net][a + u][t] * sh.d2[np][a + u];
-          float dl1 = (r4[0] + r4[1]) + (r4[2] + r4[3]);
-          dl1 *= 1.f - h1 * h1;
-          gb1 += dl1;
-#pragma unroll
-          for (int k = 0; k < kNnIn; ++k) gW1[k] += dl1 * x[k];
+            for (int k = 0; k < kNnIn; ++k) z += W1n[h][k] * xf[q][k];
+            h1[q][h] = valid[q] ? tanhf(z) : 0.f;
+          }
         }
+        // layer 2: a2[a] = b2[a] + sum_c W2[a][c] h1[c], a = lane, lane + 32
+        float a2[kOgenPB][2];
+#pragma unroll
+        for (int q = 0; q < kOgenPB; ++q) a2[q][0] = b2n[0], a2[q][1] = b2n[1];
+#pragma unroll
+        for (int hc = 0; hc < 2; ++hc)
+#pragma unroll 8
+          for (int c = 0; c < 32; ++c) {
+            const float w0 = sh.W2p[net][32 * hc + c][lane], w1 = sh.W2p[net][32 * hc + c][lane + 32];
+#pragma unroll
+            for (int q = 0; q < kOgenPB; ++q) {
+              const float hv = __shfl_sync(0xffffffffu, h1[q][hc], c);
+              a2[q][0] += w0 * hv;
+              a2[q][1] += w1 * hv;
+            }
+          }
+        float d2v[kOgenPB][2];
+#pragma unroll
+        for (int q = 0; q < kOgenPB; ++q)
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const float h2 = tanhf(a2[q][h]);
+            const float dl2 = valid[q] ? w3n[h] * (1.f - h2 * h2) : 0.f;
+            d2v[q][h] = dl2;
+            gb2[h] += dl2;
+            gw3[h] += valid[q] ? h2 : 0.f;
+            if (valid[q]) sh.d2s[warp][p0 + q][lane + 32 * h] = dl2;
+          }
+        // back to layer 1: s1[c] = sum_a W2[a][c] delta2[a], c = lane, lane + 32
+        float s1[kOgenPB][2] = {};
+#pragma unroll
+        for (int ha = 0; ha < 2; ++ha)
+#pragma unroll 8
+          for (int a = 0; a < 32; ++a) {
+            const float w0 = sh.W2p[net][lane][32 * ha + a], w1 = sh.W2p[net][lane + 32][32 * ha + a];
+#pragma unroll
+            for (int q = 0; q < kOgenPB; ++q) {
+              const float dv = __shfl_sync(0xffffffffu, d2v[q][ha], a);
+              s1[q][0] += w0 * dv;
+              s1[q][1] += w1 * dv;
+            }
+          }
+#pragma unroll
+        for (int q = 0; q < kOgenPB; ++q)
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const float dl1 = s1[q][h] * (1.f - h1[q][h] * h1[q][h]);  // zero for an invalid pair
+            gb1[h] += dl1;
+#pragma unroll
+            for (int k = 0; k < kNnIn; ++k) gW1[h][k] += dl1 * xf[q][k];
+            h1k[p0 + q][h] = h1[q][h];
+          }
+      }
+      __syncwarp();
       T* o = out + net * kNnNetP;
-#pragma unroll
-      for (int k = 0; k < kNnIn; ++k) o[kNnOffW1 + t * kNnIn + k] = gW1[k];
-      o[kNnOffB1 + t] = gb1;
-      float hc[kNnMaxPairs];
-#pragma unroll
-      for (int p = 0; p < kNnMaxPairs; ++p) hc[p] = p < np ? sh.h1[p][t] : 0.f;
+      // dJ/dW2[a][c] = sum_p delta2[p][a] h1[p][c]: lane writes columns lane and lane + 32 of each row a
+#pragma unroll 4
       for (int a = 0; a < kNnH; ++a) {
-        float g = 0.f;
+        float g0 = 0.f, g1 = 0.f;
 #pragma unroll
         for (int p = 0; p < kNnMaxPairs; ++p)
-          if (p < np) g += sh.d2[p][a] * hc[p];
-        o[kNnOffW2 + a * kNnH + t] = g;
+          if (p < np) {
+            const float dv = sh.d2s[warp][p][a];
+            g0 += dv * h1k[p][0];
+            g1 += dv * h1k[p][1];
+          }
+        o[kNnOffW2 + a * kNnH + lane] = (T)g0;
+        o[kNnOffW2 + a * kNnH + lane + 32] = (T)g1;
       }
-      o[kNnOffB2 + t] = gb2;
-      o[kNnOffW3 + t] = gw3;
-      if (t == 0) o[kNnOffB3] = (float)np;
-      __syncthreads();
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int u = lane + 32 * h;
+#pragma unroll
+        for (int k = 0; k < kNnIn; ++k) o[kNnOffW1 + u * kNnIn + k] = (T)gW1[h][k];
+        o[kNnOffB1 + u] = (T)gb1[h];
+        o[kNnOffB2 + u] = (T)gb2[h];
+        o[kNnOffW3 + u] = (T)gw3[h];
+      }
+      if (lane == 0) o[kNnOffB3] = (T)np;
+      __syncwarp();
     }
   }
 }
@@ -127,10 +212,14 @@ __global__ void __launch_bounds__(kNnH) nn_ogen_kernel(const __grid_constant__ S
 template <class T>
 static cudaError_t launch_nn_ogen_t(const SysParams<float>& sp, const double* pos, int W, int n_up, int n_elec, T* O,
                                    int ldO, int col0, int grid, cudaStream_t s) {
+  // `grid` bounds the walkers in flight (the callers pass about 3 per SM)
+  if (n_elec * (n_elec - 1) / 2 > kNnMaxPairs || n_elec * sp.n_nuc > kNnMaxPairs || 3 * n_elec > 32)
+    return cudaErrorInvalidValue;
   const size_t smem = sizeof(OgenShared);
   cudaError_t e = cudaFuncSetAttribute(nn_ogen_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  nn_ogen_kernel<T><<<grid, kNnH, smem, s>>>(sp, pos, W, n_up, n_elec, O, ldO, col0);
+  const int ctas = std::max(1, std::min((W + kOgenWarps - 1) / kOgenWarps, 2 * ((grid + 2) / 3)));
+  nn_ogen_kernel<T><<<ctas, kOgenWarps * 32, smem, s>>>(sp, pos, W, n_up, n_elec, O, ldO, col0);
   return cudaGetLastError();
 }
 cudaError_t launch_nn_ogen(const SysParams<float>& sp, const double* pos, int W, int n_up, int n_elec, float* O,
@@ -304,7 +393,7 @@ __device__ __forceinline__ void umma_commit(uint64_t* bar) {
                : "memory");
 }
 
-__global__ void __launch_bounds__(128, 1) s_gemm_kernel(const __grid_constant__ CUtensorMap tmap, double* S, int P_pad,
+__global__ void __launch_bounds__(128, 2) s_gemm_kernel(const __grid_constant__ CUtensorMap tmap, double* S, int P_pad,
                                                         int K_pad, int* status) {
   extern __shared__ __align__(1024) unsigned char gemm_smem[];
   const uintptr_t base = ((uintptr_t)gemm_smem + 1023) & ~(uintptr_t)1023;

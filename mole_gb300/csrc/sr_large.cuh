@@ -13,7 +13,7 @@ namespace mole {
 // S-matrix tiles: 128 x 128 parameters, 64 samples per pipeline stage.
 constexpr int kSBM = 128;
 constexpr int kSBK = 64;
-constexpr int kSStages = 4;
+constexpr int kSStages = 3;  // 97 KB of stages: two CTAs per SM, one's epilogue under the other's MMAs
 constexpr int kSBand = 16;  // tile rows per band of the tile order
 constexpr uint32_t kSTileBytes = kSBM * kSBK * 2;  // one BF16 operand tile, 16 KB
 constexpr size_t kSGemmSmem = 2 * kSStages * (size_t)kSTileBytes + 1024 + 256;

@@ -578,7 +578,6 @@ struct Walker {
     constexpr int i = isup ? e : e - NU;
     constexpr bool DRIFT = MOVE == kMoveDiffuse;
     constexpr int ld = isup ? NU : NDm;
-    static_assert(!(DF && DRIFT), "the df64 form has no drift-diffusion kernel");
     F* B = isup ? bu : bd;
 
     // drift at the current configuration (diffuse moves)
@@ -620,6 +619,11 @@ struct Walker {
         dx[0] = (double)step * (double)z0;
         dx[1] = (double)step * (double)z1;
         dx[2] = (double)step * (double)z2;
+      } else if constexpr (DF) {
+        const F sq = df_sqrt(step);
+        dx[0] = step * vcur[e][0] + df_mul(sq, z0);
+        dx[1] = step * vcur[e][1] + df_mul(sq, z1);
+        dx[2] = step * vcur[e][2] + df_mul(sq, z2);
       } else if constexpr (F32) {
         const float sq = sqrtf(step);
         dx[0] = (double)(step * vcur[e][0] + sq * z0);
@@ -666,20 +670,20 @@ struct Walker {
       }
     } else {
       // tentative inverse after replacing row i
-      double v[n];
+      F v[n];
 #pragma unroll
       for (int j = 0; j < n; ++j) {
-        double s = 0.0;
+        F s = F(0);
 #pragma unroll
-        for (int k = 0; k < n; ++k) s += (double)o.val[k] * B[k * ld + j];
+        for (int k = 0; k < n; ++k) s += (F)o.val[k] * B[k * ld + j];
         v[j] = s;
       }
-      const double ir = 1.0 / ratio;
+      const F ir = recip(ratio);
 #pragma unroll
       for (int k = 0; k < n; ++k) {
-        const double ck = B[k * ld + i] * ir;
+        const F ck = B[k * ld + i] * ir;
 #pragma unroll
-        for (int j = 0; j < n; ++j) bn[k * n + j] = B[k * ld + j] - ck * (v[j] - (j == i ? 1.0 : 0.0));
+        for (int j = 0; j < n; ++j) bn[k * n + j] = B[k * ld + j] - ck * (v[j] - (j == i ? F(1) : F(0)));
       }
       if constexpr (F32)
 #pragma unroll
@@ -700,7 +704,7 @@ struct Walker {
 #pragma unroll
             for (int k = 0; k < n; ++k) {
               if constexpr (F32) g += (j == e ? o.grad[k][c] : og[j][k][c]) * bnf[k * n + ij];
-              else g += (double)(j == e ? o.grad[k][c] : og[j][k][c]) * bn[k * n + ij];
+              else g += (F)(j == e ? o.grad[k][c] : og[j][k][c]) * bn[k * n + ij];
             }
             vn[c] = g;
           }
@@ -737,7 +741,7 @@ struct Walker {
         }
       });
       const D la = (D)2 * (D)dJ - (hi - lo) / ((D)2 * (D)step);
-      acc = (ratio > 0.0) && metropolis_accept(ratio, (double)la, ubits);
+      acc = is_pos(ratio) && metropolis_accept(ratio, (F)la, ubits);
     }
     if (!acc) return 0;
 
@@ -753,6 +757,12 @@ struct Walker {
     if constexpr (DRIFT) {
 #pragma unroll
       for (int k = 0; k < n * n; ++k) B[(k / n) * ld + (k % n)] = bn[k];
+      if constexpr (DF) {
+        bool in = true;
+#pragma unroll
+        for (int k = 0; k < n * n; ++k) in = in && (piv_mag(bn[k]) < 0x1p96f);
+        if (!in) oor = true;
+      }
       if constexpr (F32) {
         float* Bf = isup ? bfu : bfd;
 #pragma unroll

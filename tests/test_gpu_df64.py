@@ -130,3 +130,48 @@ def test_df64_out_of_range_walker_reruns_in_fp64(ctx):
     assert ctx.df64_reruns() == before + 1
     r = O.evaluate(s, pos, want_O=False)
     assert close(g["eloc"], r["eloc"]) < RTOL
+
+
+@pytest.mark.parametrize("name,tau", [("He", 0.02), ("Be", 0.005), ("H2", 0.01)])
+def test_df64_dmc_trajectory_matches_oracle(ctx, name, tau):
+    s = systems()[name]
+    wf = api.WaveFunction(ctx, s)
+    W = 300
+    wk = api.Walkers(wf, W, seed=77)
+    pos = wk.positions()
+    el = O.evaluate(s, pos, want_O=False)["eloc"]
+    dmc = api.DmcRunner(wf, wk, reference_energy=-1.0, precision=api.PREC_DF64)
+    before = ctx.df64_reruns()
+    e_gpu = dmc.run_block(tau, 6)
+    assert ctx.df64_reruns() == before
+    e_ref = []
+    acc = 0.0
+    for t in range(6):
+        r = O.dmc_step(s, pos, el, tau=tau, e_ref=-1.0, seed=77, step=t)
+        pos, el = r["pos"], r["eloc"]
+        e_ref.append(r["energy"])
+        acc += r["accepted"]
+    assert close(e_gpu, e_ref, rtol=1e-9) < 1e-9
+    assert close(wk.positions(), pos, rtol=1e-9) < 1e-9
+    assert dmc.accepted == acc
+
+
+def test_df64_dmc_far_walker_reruns_in_fp64(ctx):
+    """A Be walker with an electron 300 bohr out: the double-float DMC steps
+    are rerun in native FP64 and give the native result."""
+    s = systems()["Be"]
+    wf = api.WaveFunction(ctx, s)
+    W = 128
+    pos = np.random.default_rng(4).normal(size=(W, 4, 3))
+    pos[7, 3] = [0.0, 300.0, 0.0]
+    out = {}
+    for prec in (api.PREC_FP64, api.PREC_DF64):
+        wk = api.Walkers(wf, W, seed=8)
+        wk.set_positions(pos)
+        dmc = api.DmcRunner(wf, wk, reference_energy=-14.6, precision=prec)
+        before = ctx.df64_reruns()
+        e = dmc.run_block(0.005, 4)
+        out[prec] = (np.asarray(e), wk.positions(), ctx.df64_reruns() - before)
+    assert out[api.PREC_FP64][2] == 0 and out[api.PREC_DF64][2] == 1
+    np.testing.assert_array_equal(out[api.PREC_DF64][0], out[api.PREC_FP64][0])
+    np.testing.assert_array_equal(out[api.PREC_DF64][1], out[api.PREC_FP64][1])
