@@ -85,7 +85,8 @@ class Context:
 
     def math_check(self, fn: int, x) -> np.ndarray:
         """The library's device arithmetic on x (0: FP64 exp of the native kernels,
-        1-4: double-float exp, rsqrt, reciprocal, x / (1 + x^2))."""
+        1-4: double-float exp, rsqrt, reciprocal, x / (1 + x^2); 5, 6: the
+        integer-built float -> double and double -> float (toward zero) conversions)."""
         x = np.ascontiguousarray(x, dtype=np.float64)
         y = np.empty_like(x)
         check(self.lib.mole_math_check(self.h, fn, dptr(x), x.size, dptr(y)))

@@ -76,6 +76,18 @@ __host__ __device__ inline int batch_slots(int nu, int nd) {
   return (sizeof(R) == sizeof(double) ? 3 * (nu + nd) : 0) + nu * nu + nd * nd;
 }
 
+// R -> double and float -> R without an FP64-pipe conversion (f2d is exact).
+template <class R>
+__device__ __forceinline__ double up_d(R v) {
+  if constexpr (sizeof(R) == sizeof(double)) return v;
+  else return f2d(v);
+}
+template <class R>
+__device__ __forceinline__ R from_f(float v) {
+  if constexpr (sizeof(R) == sizeof(double)) return f2d(v);
+  else return v;
+}
+
 // a / b: IEEE in FP64, the SFU reciprocal (2 ulp) in the FP32 form.
 template <class R>
 __device__ __forceinline__ R div_t(R a, R b) {
@@ -183,7 +195,7 @@ __device__ bool batch_refresh(const SysParams<R>& sp, const BatchWalker<R>& wk) 
         R phi[kMaxSpin], jen;
         batch_orbitals<R>(sp, spin, r, phi, jen);
 #pragma unroll
-        for (int k = 0; k < kMaxSpin; ++k) a[i][k] = (double)phi[k];
+        for (int k = 0; k < kMaxSpin; ++k) a[i][k] = up_d<R>(phi[k]);
       } else {
 #pragma unroll
         for (int k = 0; k < kMaxSpin; ++k) a[i][k] = 0.0;
@@ -268,7 +280,7 @@ __device__ __forceinline__ int batch_move(const SysParams<R>& sp, const BatchWal
     uacc = u01<R>(rb.x);
     ubits = rb.x;
 #pragma unroll
-    for (int c = 0; c < 3; ++c) dx[c] = step * (R)z[c];
+    for (int c = 0; c < 3; ++c) dx[c] = step * from_f<R>(z[c]);
   }
   const R ro[3] = {wk.xr(e, 0), wk.xr(e, 1), wk.xr(e, 2)};
   R rn[3];
@@ -292,7 +304,7 @@ __device__ __forceinline__ int batch_move(const SysParams<R>& sp, const BatchWal
   double ratio = 0.0;
 #pragma unroll
   for (int k = 0; k < kMaxSpin; ++k)
-    if (k < n) ratio += (double)phi[k] * B[(k * n + i) * nt];
+    if (k < n) ratio += up_d<R>(phi[k]) * B[(k * n + i) * nt];
   R dJ = jn - jo;
   for (int j = 0; j < N; ++j) {
     if (j == e) continue;
@@ -304,7 +316,7 @@ __device__ __forceinline__ int batch_move(const SysParams<R>& sp, const BatchWal
   if constexpr (F64) {
     if (!metropolis_accept(ratio, 2.0 * dJ, ubits)) return 0;
   } else {
-    const float rf = (float)ratio;  // the acceptance test itself is a random comparison: FP32
+    const float rf = d2f_rz(ratio);  // the acceptance test itself is a random comparison: FP32
     if (!(rf * rf * __expf(2.0f * dJ) > uacc)) return 0;
   }
 
@@ -314,7 +326,7 @@ __device__ __forceinline__ int batch_move(const SysParams<R>& sp, const BatchWal
     for (int c = 0; c < 3; ++c) wk.set_x(e, c, xn[c]);
   } else {
 #pragma unroll
-    for (int c = 0; c < 3; ++c) wk.set_x(e, c, xn[c] + (double)dx[c]);
+    for (int c = 0; c < 3; ++c) wk.set_x(e, c, xn[c] + up_d<R>(dx[c]));
   }
   double v[kMaxSpin], col[kMaxSpin];
   double* Bw = wk.B(spin);
@@ -324,7 +336,7 @@ __device__ __forceinline__ int batch_move(const SysParams<R>& sp, const BatchWal
     double s = 0.0;
 #pragma unroll
     for (int k = 0; k < kMaxSpin; ++k)
-      if (k < n) s += (double)phi[k] * Bw[(k * n + j) * nt];
+      if (k < n) s += up_d<R>(phi[k]) * Bw[(k * n + j) * nt];
     v[j] = s - (j == i ? 1.0 : 0.0);
   }
   const double ir = 1.0 / ratio;
@@ -362,10 +374,10 @@ __device__ double batch_local_energy(const SysParams<R>& sp, const BatchWalker<R
     for (int k = 0; k < kMaxSpin; ++k)
       if (k < n) {
         const double b = B[(k * n + i) * nt];
-        gD[0] += (double)o.grad[k][0] * b;
-        gD[1] += (double)o.grad[k][1] * b;
-        gD[2] += (double)o.grad[k][2] * b;
-        lD += (double)o.lap[k] * b;
+        gD[0] += up_d<R>(o.grad[k][0]) * b;
+        gD[1] += up_d<R>(o.grad[k][1]) * b;
+        gD[2] += up_d<R>(o.grad[k][2]) * b;
+        lD += up_d<R>(o.lap[k]) * b;
       }
     R gJ[3] = {o.gjen[0], o.gjen[1], o.gjen[2]};
     R lJ = o.ljen, Ve = o.ven;
@@ -382,9 +394,9 @@ __device__ double batch_local_energy(const SysParams<R>& sp, const BatchWalker<R
     }
     // the electron's Jastrow-only terms in R, the determinant terms in FP64
     const R jj = lJ + gJ[0] * gJ[0] + gJ[1] * gJ[1] + gJ[2] * gJ[2];
-    const double dot = gD[0] * (double)gJ[0] + gD[1] * (double)gJ[1] + gD[2] * (double)gJ[2];
-    lap += lD + (double)jj + 2.0 * dot;
-    V += (double)Ve;
+    const double dot = gD[0] * up_d<R>(gJ[0]) + gD[1] * up_d<R>(gJ[1]) + gD[2] * up_d<R>(gJ[2]);
+    lap += lD + up_d<R>(jj) + 2.0 * dot;
+    V += up_d<R>(Ve);
   }
   return -0.5 * lap + V;
 }

@@ -24,9 +24,10 @@
 // exp64 is an FP64 exponential for the native FP64 kernels built on the same
 // pieces: FP64 argument reduction, e^r - 1 in double-float (small enough that
 // 2^-47 relative is below half an FP64 ulp of the result), one FP64 FMA to
-// finish. Five FP64-pipe instructions instead of the library's fifteen
-// (measured with the FP64-pipe instruction counter); float <-> double
-// conversions do not use the FP64 pipe.
+// finish: five FP64-pipe instructions against the library's fifteen (counted
+// with smsp__inst_executed_pipe_fp64 in a microbenchmark), its float <-> double
+// conversions done with integer operations (f2d, d2f_rz below), since a
+// hardware conversion takes an FP64-pipe slot like a DADD.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -38,6 +39,37 @@
 #include "common.cuh"
 
 namespace mole {
+
+// float <-> double conversions and double comparisons each take an FP64-pipe
+// slot on GB300 (one warp instruction per 16 cycles per SM), as much as a
+// DFMA. The two below build the result with integer operations and selects
+// only (no branch the compiler could if-convert into a hardware conversion).
+//
+// float -> double: exponent rebiased by 1023 - 127, significand shifted into
+// place; exact for normal floats, zeros, infinities and NaNs; subnormal
+// floats (below 1.2e-38 in magnitude) become zeros of their sign.
+__device__ __forceinline__ double f2d(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t s = u & 0x80000000u, e = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu;
+  uint32_t hi = s | ((e + 896u) << 20) | (m >> 3);
+  uint32_t lo = m << 29;
+  hi = e == 0xFFu ? (s | 0x7FF00000u | (m >> 3)) : hi;
+  hi = e == 0u ? s : hi;
+  lo = e == 0u ? 0u : lo;
+  return __hiloint2double((int)hi, (int)lo);
+}
+// double -> float rounded toward zero (the top 24 significant bits); values
+// below FP32's normal range become zeros of their sign, values above it
+// infinities, NaNs stay NaNs.
+__device__ __forceinline__ float d2f_rz(double d) {
+  const uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
+  const uint32_t s = hi & 0x80000000u, e = (hi >> 20) & 0x7FFu;
+  const uint32_t m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+  uint32_t u = s | ((e - 896u) << 23) | m;
+  u = e > 1150u ? (s | 0x7F800000u | (e == 0x7FFu ? (m | (lo != 0u)) : 0u)) : u;
+  u = e < 897u ? s : u;
+  return __uint_as_float(u);
+}
 
 struct df64 {
   float h, l;
@@ -249,16 +281,17 @@ __device__ __forceinline__ df64 df_exp(df64 x) {
 // below 2^-54); e^x = 2^(n >> 6) (T + T q), T = 2^((n & 63)/64). Outside
 // |x| < 700 (overflow, subnormal results) the library exp.
 __device__ __forceinline__ double exp64(double x) {
-  const float xf = __double2float_rn(x);
+  const float xf = d2f_rz(x);
   if (!(fabsf(xf) < 700.f)) return exp(x);
   constexpr double kL1 = 0x1.62e42fefa0000p-7;
   constexpr double kL2 = 0x1.cf79abc9e3b3ap-46;
   const float n = rintf(__fmul_rn(xf, 92.33248261689366f));
-  const double nd = (double)n;
+  const double nd = f2d(n);
   double r = fma(-nd, kL1, x);
   r = fma(-nd, kL2, r);
-  const float rh = __double2float_rn(r);
-  const df64 rd(rh, __double2float_rn(r - (double)rh));
+  // r as a double-float: its top 24 bits, then the (exact) remainder's
+  const float rh = d2f_rz(r);
+  const df64 rd(rh, d2f_rz(r - f2d(rh)));
   float t = __fmaf_rn(rh, 1.0f / 720.0f, 1.0f / 120.0f);
   t = __fmaf_rn(rh, t, 1.0f / 24.0f);
   const df64 a = df_mul(rd, t) + df64(0x1.555556p-3f, -0x1.555556p-28f);  // 1/6 + r t
@@ -266,7 +299,7 @@ __device__ __forceinline__ double exp64(double x) {
   const df64 q = rd + rd * (rd * b);
   const int ni = (int)n;
   const double T = __ldg(&kExp2Tab64[ni & 63]);
-  const double v = fma(T, (double)q.h + (double)q.l, T);
+  const double v = fma(T, f2d(q.h) + f2d(q.l), T);
   // scale by 2^(n >> 6) in the exponent field (v is in [1, 2.1), the result normal)
   return __hiloint2double(__double2hiint(v) + (ni >> 6) * (1 << 20), __double2loint(v));
 }

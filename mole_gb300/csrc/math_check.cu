@@ -1,7 +1,8 @@
 // math_check.cu -- evaluates the library's own device arithmetic on arrays so
 // that tests can pin its accuracy: the FP64 exponential of the native FP64
-// kernels and the double-float exp, reciprocal square root and reciprocal of
-// the double-float kernels.
+// kernels, the double-float exp, reciprocal square root and reciprocal of
+// the double-float kernels, and the integer-built float <-> double
+// conversions.
 #include "df64.cuh"
 
 namespace mole {
@@ -16,7 +17,9 @@ __global__ void math_check_kernel(int fn, const double* x, int64_t n, double* y)
     case 1: r = (double)df_exp(df64(v)); break;
     case 2: r = (double)df_rsqrt(df64(v)); break;
     case 3: r = (double)df_rcp(df64(v)); break;
-    default: r = (double)(df64(v) / df64(1.0 + v * v)); break;
+    case 4: r = (double)(df64(v) / df64(1.0 + v * v)); break;
+    case 5: r = f2d(__double2float_rn(v)); break;
+    default: r = (double)d2f_rz(v); break;
   }
   y[i] = r;
 }

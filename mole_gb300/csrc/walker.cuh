@@ -270,15 +270,16 @@ __device__ __forceinline__ void pair_vals(const SysParams<R>& sp, bool same, R d
 }
 
 // The Metropolis test ratio^2 exp(x) > u, u = u01(ubits) >= 2^-33. With
-// |x| < 80 and 1e-30 < ratio^2 < 1e30 the FP32 value of ratio^2 exp(x) is
-// within 2e-5 relative of the exact one while it is a normal float, and it
+// |x| < 80 and 1e-30 < ratio^2 < 1e30 the FP32 value of ratio^2 exp(x) (from
+// ratio and x truncated to 24 bits) is within 3e-5 relative of the exact one
+// while it is a normal float, and it
 // under- (over-) flows only when the exact value is below 1e-38 (above
 // 3e38), i.e. far below (above) any u; so where it is clear of u by 1e-3
 // relative it decides exactly as the FP64 test. Everything else takes the
 // FP64 expression. Same decisions as FP64, the FP64 exp skipped in all but
 // borderline and extreme cases.
 __device__ __forceinline__ bool metropolis_accept(double ratio, double x, uint32_t ubits) {
-  const float rf = (float)ratio, xf = (float)x;
+  const float rf = d2f_rz(ratio), xf = d2f_rz(x);  // truncated: no FP64-pipe conversion
   const float r2 = rf * rf;
   if (fabsf(xf) < 80.f && r2 > 1e-30f && r2 < 1e30f) {
     const float uf = u01<float>(ubits);
@@ -383,6 +384,17 @@ struct Walker {
   static constexpr bool DF = is_df64<R>::value;
   using F = typename std::conditional<DF, df64, double>::type;
 
+  // R -> F and F -> R for the FP32 form without FP64-pipe conversions (f2d is
+  // exact; d2f_rz truncates to 24 bits); identities otherwise
+  static __device__ __forceinline__ F to_f(R v) {
+    if constexpr (F32) return f2d(v);
+    else return (F)v;
+  }
+  static __device__ __forceinline__ R to_r(F v) {
+    if constexpr (F32) return d2f_rz(v);
+    else return (R)v;
+  }
+
   F x[N][3];
   F bu[NU * NU];    // inverse of the up Slater matrix, bu[k*NU+i]
   F bd[NDm * NDm];  // inverse of the down Slater matrix
@@ -421,9 +433,9 @@ struct Walker {
       for (int c = 0; c < 3; ++c) pos[(size_t)(3 * e + c) * W + w] = to_d(x[e][c]);
   }
   __device__ __forceinline__ void rpos(int e, R (&r)[3]) const {
-    r[0] = (R)x[e][0];
-    r[1] = (R)x[e][1];
-    r[2] = (R)x[e][2];
+    r[0] = to_r(x[e][0]);
+    r[1] = to_r(x[e][1]);
+    r[2] = to_r(x[e][2]);
   }
 
   template <int e, int n>
@@ -482,9 +494,9 @@ struct Walker {
     if constexpr (ND > 0) ok = gj_invert<ND>(ad, bd, lndet ? &l2 : nullptr, &s2) && ok;
     if constexpr (F32) {
 #pragma unroll
-      for (int k = 0; k < NU * NU; ++k) bfu[k] = (float)bu[k];
+      for (int k = 0; k < NU * NU; ++k) bfu[k] = d2f_rz(bu[k]);
 #pragma unroll
-      for (int k = 0; k < (ND > 0 ? ND * ND : 0); ++k) bfd[k] = (float)bd[k];
+      for (int k = 0; k < (ND > 0 ? ND * ND : 0); ++k) bfd[k] = d2f_rz(bd[k]);
     }
     if constexpr (DF) check_range<NU>(bu), check_range<ND>(bd);
     F J = F(0);
@@ -530,7 +542,7 @@ struct Walker {
     for (int c = 0; c < 3; ++c) {
       F s = F(0);
 #pragma unroll
-      for (int k = 0; k < n; ++k) s += (F)og[j][k][c] * B[k * ld + i];
+      for (int k = 0; k < n; ++k) s += to_f(og[j][k][c]) * B[k * ld + i];
       g[c] = s;
     }
   }
@@ -564,9 +576,9 @@ struct Walker {
     for (int m = 0; m < N; ++m) {
       if (m == j) continue;
       const R f = pf[pidx(j, m)];
-      g[0] += f * (R)(x[j][0] - x[m][0]);
-      g[1] += f * (R)(x[j][1] - x[m][1]);
-      g[2] += f * (R)(x[j][2] - x[m][2]);
+      g[0] += f * to_r(x[j][0] - x[m][0]);
+      g[1] += f * to_r(x[j][1] - x[m][1]);
+      g[2] += f * to_r(x[j][2] - x[m][2]);
     }
   }
 
@@ -616,9 +628,9 @@ struct Walker {
         dx[1] = df_mul(step, z1);
         dx[2] = df_mul(step, z2);
       } else if constexpr (MOVE == kMoveGauss) {
-        dx[0] = (double)step * (double)z0;
-        dx[1] = (double)step * (double)z1;
-        dx[2] = (double)step * (double)z2;
+        dx[0] = (double)step * f2d(z0);
+        dx[1] = (double)step * f2d(z1);
+        dx[2] = (double)step * f2d(z2);
       } else if constexpr (DF) {
         const F sq = df_sqrt(step);
         dx[0] = step * vcur[e][0] + df_mul(sq, z0);
@@ -626,9 +638,9 @@ struct Walker {
         dx[2] = step * vcur[e][2] + df_mul(sq, z2);
       } else if constexpr (F32) {
         const float sq = sqrtf(step);
-        dx[0] = (double)(step * vcur[e][0] + sq * z0);
-        dx[1] = (double)(step * vcur[e][1] + sq * z1);
-        dx[2] = (double)(step * vcur[e][2] + sq * z2);
+        dx[0] = f2d(step * vcur[e][0] + sq * z0);
+        dx[1] = f2d(step * vcur[e][1] + sq * z1);
+        dx[2] = f2d(step * vcur[e][2] + sq * z2);
       } else {
         const double sq = sqrt((double)step);
         dx[0] = (double)step * vcur[e][0] + sq * (double)z0;
@@ -642,7 +654,7 @@ struct Walker {
     one_body<R, n, NZ, EN, NN>(sp, isup ? 0 : 1, rn, o, &nn);
     F ratio = F(0);
 #pragma unroll
-    for (int k = 0; k < n; ++k) ratio += (F)o.val[k] * B[k * ld + i];
+    for (int k = 0; k < n; ++k) ratio += to_f(o.val[k]) * B[k * ld + i];
 
     // new pair terms of electron e
     R dJ = o.jen - jen[e];
@@ -650,7 +662,7 @@ struct Walker {
     static_for<0, N>([&](auto jc) {
       constexpr int j = decltype(jc)::value;
       if constexpr (j != e) {
-        pair_vals<R, PM, NN>(sp, same_spin(e, j), rn[0] - (R)x[j][0], rn[1] - (R)x[j][1], rn[2] - (R)x[j][2], pv[j],
+        pair_vals<R, PM, NN>(sp, same_spin(e, j), rn[0] - to_r(x[j][0]), rn[1] - to_r(x[j][1]), rn[2] - to_r(x[j][2]), pv[j],
                              &nn);
         dJ += pv[j].u - pu[pidx(e, j)];
       }
@@ -665,8 +677,15 @@ struct Walker {
       } else if constexpr (DF) {
         acc = metropolis_accept(ratio, twice(dJ), ubits);
       } else {
-        const double p = ratio * ratio * (double)exp_t<R>((R)2 * dJ);
-        acc = p > (double)uacc;
+        // ratio^2 e^(2 dJ) > u screened in FP32 (the truncated ratio is within
+        // 2^-23, the product within about 2.4e-7 relative), the FP64
+        // expression deciding only within 1e-3 of u: the same decisions
+        const float ef = exp_t<R>((R)2 * dJ);
+        const float rf = d2f_rz(ratio);
+        const float r2 = rf * rf;
+        const float dd = r2 * ef - uacc;
+        if (r2 > 1e-30f && r2 < 1e30f && ef < 1e30f && fabsf(dd) > 1e-3f * uacc) acc = dd > 0.f;
+        else acc = ratio * ratio * f2d(ef) > f2d(uacc);
       }
     } else {
       // tentative inverse after replacing row i
@@ -675,7 +694,7 @@ struct Walker {
       for (int j = 0; j < n; ++j) {
         F s = F(0);
 #pragma unroll
-        for (int k = 0; k < n; ++k) s += (F)o.val[k] * B[k * ld + j];
+        for (int k = 0; k < n; ++k) s += to_f(o.val[k]) * B[k * ld + j];
         v[j] = s;
       }
       const F ir = recip(ratio);
@@ -687,7 +706,7 @@ struct Walker {
       }
       if constexpr (F32)
 #pragma unroll
-        for (int k = 0; k < n * n; ++k) bnf[k] = (float)bn[k];
+        for (int k = 0; k < n * n; ++k) bnf[k] = d2f_rz(bn[k]);
       // Green's function ratio over every electron (metrop.rs:182-195) with
       // the drift at the proposed configuration
       D hi = 0, lo = 0;
@@ -720,20 +739,20 @@ struct Walker {
 #pragma unroll
           for (int m = 0; m < N; ++m) {
             if (m == e) continue;
-            gj[0] += pv[m].f * (rn[0] - (R)x[m][0]);
-            gj[1] += pv[m].f * (rn[1] - (R)x[m][1]);
-            gj[2] += pv[m].f * (rn[2] - (R)x[m][2]);
+            gj[0] += pv[m].f * (rn[0] - to_r(x[m][0]));
+            gj[1] += pv[m].f * (rn[1] - to_r(x[m][1]));
+            gj[2] += pv[m].f * (rn[2] - to_r(x[m][2]));
           }
         } else {
           jas_grad<j>(gj);
           const R fo = pf[pidx(j, e)], fn = pv[j].f;
-          gj[0] += fn * ((R)x[j][0] - rn[0]) - fo * (R)(x[j][0] - x[e][0]);
-          gj[1] += fn * ((R)x[j][1] - rn[1]) - fo * (R)(x[j][1] - x[e][1]);
-          gj[2] += fn * ((R)x[j][2] - rn[2]) - fo * (R)(x[j][2] - x[e][2]);
+          gj[0] += fn * (to_r(x[j][0]) - rn[0]) - fo * to_r(x[j][0] - x[e][0]);
+          gj[1] += fn * (to_r(x[j][1]) - rn[1]) - fo * to_r(x[j][1] - x[e][1]);
+          gj[2] += fn * (to_r(x[j][2]) - rn[2]) - fo * to_r(x[j][2] - x[e][2]);
         }
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          const D dj = (j == e) ? (D)dx[c] : (D)0;
+          const D dj = (j == e) ? to_r(dx[c]) : (D)0;  // D is R in every form
           const D a = -dj - (D)step * (vn[c] + (D)gj[c]);
           const D b = dj - (D)step * vcur[j][c];
           hi += a * a;
@@ -741,7 +760,7 @@ struct Walker {
         }
       });
       const D la = (D)2 * (D)dJ - (hi - lo) / ((D)2 * (D)step);
-      acc = is_pos(ratio) && metropolis_accept(ratio, (F)la, ubits);
+      acc = is_pos(ratio) && metropolis_accept(ratio, to_f(la), ubits);
     }
     if (!acc) return 0;
 
@@ -775,7 +794,7 @@ struct Walker {
       for (int j = 0; j < n; ++j) {
         F s = F(0);
 #pragma unroll
-        for (int k = 0; k < n; ++k) s += (F)o.val[k] * B[k * ld + j];
+        for (int k = 0; k < n; ++k) s += to_f(o.val[k]) * B[k * ld + j];
         v[j] = s;
       }
       const F ir = recip(ratio);
@@ -824,7 +843,7 @@ struct Walker {
       F gD[3], lD = F(0);
       det_grad<e>(gD);
 #pragma unroll
-      for (int k = 0; k < n; ++k) lD += (F)ol[e][k] * B[k * ld + i];
+      for (int k = 0; k < n; ++k) lD += to_f(ol[e][k]) * B[k * ld + i];
       R gJ[3];
       jas_grad<e>(gJ);
       R lJ = ljen[e];
@@ -834,28 +853,28 @@ struct Walker {
       F dot = F(0), gj2 = F(0);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const F gj = (F)gJ[c];
+        const F gj = to_f(gJ[c]);
         dot += gD[c] * gj;
         gj2 += gj * gj;
         if (grad) grad[3 * e + c] = to_d(gD[c] + gj);
       }
-      lap += lD + (F)lJ + twice(dot) + gj2;
-      if (sp.pot_kind == 0) V += (F)ven[e];
-      else V += (F)sp.half_omega2 * (x[e][0] * x[e][0] + x[e][1] * x[e][1] + x[e][2] * x[e][2]);
+      lap += lD + to_f(lJ) + twice(dot) + gj2;
+      if (sp.pot_kind == 0) V += to_f(ven[e]);
+      else V += to_f(sp.half_omega2) * (x[e][0] * x[e][0] + x[e][1] * x[e][1] + x[e][2] * x[e][2]);
       if constexpr (PM > 0) {
 #pragma unroll
         for (int p = 0; p < PM; ++p) {
           F s = F(0);
 #pragma unroll
-          for (int k = 0; k < n; ++k) s += (F)odz[e][k][p] * B[k * ld + i];
+          for (int k = 0; k < n; ++k) s += to_f(odz[e][k][p]) * B[k * ld + i];
           O[p] += s;
         }
-        djs += (F)djen[e];
+        djs += to_f(djen[e]);
       }
     });
     if (sp.pot_kind == 0) {
 #pragma unroll
-      for (int p = 0; p < NP; ++p) V += (F)pinv[p];
+      for (int p = 0; p < NP; ++p) V += to_f(pinv[p]);
       if constexpr (DF) V += sp.vnn_r;
       else V += sp.vnn;
     }
@@ -863,13 +882,13 @@ struct Walker {
       F dudb = F(0), dpoly[kMaxPoly] = {F(0), F(0), F(0), F(0)};
 #pragma unroll
       for (int p = 0; p < NP; ++p) {
-        dudb += (F)pdb[p];
+        dudb += to_f(pdb[p]);
         // d u / d b_(q+3) = R^(q+2)
-        F rk = (F)prs[p] * (F)prs[p];
+        F rk = to_f(prs[p]) * to_f(prs[p]);
         #pragma unroll 1
         for (int q = 0; q < sp.ee_npoly; ++q) {
           dpoly[q] += rk;
-          rk *= (F)prs[p];
+          rk *= to_f(prs[p]);
         }
       }
 #pragma unroll

@@ -40,3 +40,32 @@ def test_double_float_functions_within_2_pow_44(ctx, fn, lo, hi, kind):
     y = ctx.math_check(fn, x)
     rel = np.abs(y - ref) / np.abs(ref)
     assert rel.max() < 2.0 ** -44, rel.max()
+
+
+def test_integer_built_conversions(ctx):
+    """f2d is exact for normal floats, zeros, infinities and NaNs (subnormals
+    become signed zeros); d2f_rz keeps the top 24 bits (rounds toward zero)
+    inside FP32's normal range, flushes below it and saturates to infinity
+    above it."""
+    rng = np.random.default_rng(17)
+    x = np.concatenate([rng.normal(0.0, 1.0, 20000) * 10.0 ** rng.integers(-30, 30, 20000),
+                        [0.0, -0.0, 1.0, -1.0, 3.4e38, -3.4e38, 1e-39, -1e-39, 1e-300, 1e300, np.inf, -np.inf, np.nan]])
+    y = ctx.math_check(5, x)
+    with np.errstate(over="ignore"):
+        f = x.astype(np.float32)
+    ref = np.where(np.abs(f) < np.finfo(np.float32).tiny, np.copysign(0.0, f), f).astype(np.float64)
+    fin = ~np.isnan(x)
+    np.testing.assert_array_equal(y[fin], ref[fin])
+    np.testing.assert_array_equal(np.signbit(y[fin]), np.signbit(ref[fin]))
+    assert np.isnan(y[~fin]).all()
+    z = ctx.math_check(6, x)
+    assert np.isnan(z[~fin]).all()
+    z, xf = z[fin], x[fin]
+    tiny, big = float(np.finfo(np.float32).tiny), float(np.finfo(np.float32).max)
+    normal = (np.abs(xf) >= tiny) & (np.abs(xf) <= big)
+    zn, xn = z[normal], xf[normal]
+    assert np.array_equal(zn.astype(np.float32).astype(np.float64), zn)  # representable in FP32
+    assert np.all(np.abs(zn) <= np.abs(xn)) and np.all(np.sign(zn) == np.sign(xn))
+    assert np.all(np.abs(xn - zn) < np.spacing(np.abs(zn).astype(np.float32)).astype(np.float64))
+    assert np.all(z[np.abs(xf) < tiny] == 0.0)
+    assert np.all(np.isinf(z[np.abs(xf) > big]))
