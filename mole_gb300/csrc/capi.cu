@@ -337,7 +337,7 @@ int mole_ctx_kernel_time(mole_ctx* c, int32_t kernel, double* total_ms, int64_t*
 
 int mole_math_check(mole_ctx* c, int32_t fn, const double* x, int64_t n, double* y) {
   cudaGetLastError();
-  if (!c || !x || !y || n < 0 || fn < 0 || fn > 6) return fail(MOLE_ERR_INVALID_ARG, "bad argument");
+  if (!c || !x || !y || n < 0 || fn < 0 || fn > 7) return fail(MOLE_ERR_INVALID_ARG, "bad argument");
   CUDA_TRY(c->scratch.reserve((size_t)2 * std::max<int64_t>(n, 1)));
   double* dx = c->scratch.p;
   double* dy = dx + n;

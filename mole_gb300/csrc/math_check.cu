@@ -19,7 +19,8 @@ __global__ void math_check_kernel(int fn, const double* x, int64_t n, double* y)
     case 3: r = (double)df_rcp(df64(v)); break;
     case 4: r = (double)(df64(v) / df64(1.0 + v * v)); break;
     case 5: r = f2d(__double2float_rn(v)); break;
-    default: r = (double)d2f_rz(v); break;
+    case 6: r = (double)d2f_rz(v); break;
+    default: r = (double)d2f_rz_small(v); break;
   }
   y[i] = r;
 }

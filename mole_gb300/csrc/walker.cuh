@@ -391,7 +391,7 @@ struct Walker {
     else return (F)v;
   }
   static __device__ __forceinline__ R to_r(F v) {
-    if constexpr (F32) return d2f_rz(v);
+    if constexpr (F32) return d2f_rz_small(v);  // positions: below FP32's largest
     else return (R)v;
   }
 
@@ -649,7 +649,7 @@ struct Walker {
       }
     }
     const F xn[3] = {x[e][0] + dx[0], x[e][1] + dx[1], x[e][2] + dx[2]};
-    const R rn[3] = {(R)xn[0], (R)xn[1], (R)xn[2]};
+    const R rn[3] = {to_r(xn[0]), to_r(xn[1]), to_r(xn[2])};  // as every other FP32 position
     OneBody<R, n, NZ> o;
     one_body<R, n, NZ, EN, NN>(sp, isup ? 0 : 1, rn, o, &nn);
     F ratio = F(0);

@@ -69,3 +69,6 @@ def test_integer_built_conversions(ctx):
     assert np.all(np.abs(xn - zn) < np.spacing(np.abs(zn).astype(np.float32)).astype(np.float64))
     assert np.all(z[np.abs(xf) < tiny] == 0.0)
     assert np.all(np.isinf(z[np.abs(xf) > big]))
+    # the variant for positions agrees wherever its input is below FP32's largest
+    small = np.abs(xf) <= big
+    np.testing.assert_array_equal(ctx.math_check(7, xf[small]), z[small])
