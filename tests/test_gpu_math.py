@@ -4,7 +4,9 @@ The native FP64 kernels use an FP64 exponential of their own (FP64 argument
 reduction, e^r - 1 in double-float on the FP32 pipe, one FP64 FMA to finish);
 it stays within 3 ulp of numpy's exp. The double-float kernels' exp,
 reciprocal square root, reciprocal and quotient stay within 2^-44 relative
-(double-float carries about 48 bits).
+(double-float carries about 48 bits). The float <-> double conversions built
+from integer operations (which keep conversions off GB300's FP64 pipe) are
+exact, or keep the top 24 bits, as documented.
 """
 import numpy as np
 import pytest
