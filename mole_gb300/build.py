@@ -68,8 +68,8 @@ def build(jobs: int | None = None, verbose: bool = False) -> str:
     # so the parallel build finishes sooner
     def weight(s: str) -> int:
         b = os.path.basename(s)
-        return (os.path.getsize(s) + 100000 * ("_2_2" in b) + 60000 * ("inst_df" in b) + 40000 * ("_2_1" in b)
-                + 200000 * (b == "capi.cu"))
+        return (os.path.getsize(s) + 100000 * ("_2_2" in b) + 60000 * ("inst_df" in b or "inst_nn" in b)
+                + 40000 * ("_2_1" in b) + 200000 * (b == "capi.cu"))
 
     srcs.sort(key=lambda s: -weight(s))
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:

@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <initializer_list>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -11,9 +12,36 @@
 #include "handles.cuh"
 
 namespace mole {
-#define MOLE_DECL(NU, ND)                           \
-  const KernelSetT<double>* kernels_f64_##NU##_##ND(); \
-  const KernelSetT<float>* kernels_f32_##NU##_##ND();
+// A family's kernel set from the slices its translation units compile.
+template <class R>
+KernelSetT<R> merge_parts(std::initializer_list<KernelSetT<R>> parts) {
+  KernelSetT<R> k{};
+  for (const KernelSetT<R>& p : parts) {
+    for (int a = 0; a < kPmSlots; ++a)
+      for (int d = 0; d < 2; ++d)
+        for (int e = 0; e < 2; ++e)
+          if (p.vmc[a][d][e]) k.vmc[a][d][e] = p.vmc[a][d][e];
+    for (int e = 0; e < 2; ++e) {
+      if (p.eval[e]) k.eval[e] = p.eval[e];
+      if (p.dmc[e]) k.dmc[e] = p.dmc[e];
+    }
+  }
+  return k;
+}
+#define MOLE_DECL_PARTS(NU, ND, R, TAG)                                                   \
+  KernelSetT<R> kparts_##TAG##_##NU##_##ND##_0();                                         \
+  KernelSetT<R> kparts_##TAG##_##NU##_##ND##_1();                                         \
+  KernelSetT<R> kparts_##TAG##_##NU##_##ND##_2();                                         \
+  KernelSetT<R> kparts_##TAG##_##NU##_##ND##_r();                                         \
+  const KernelSetT<R>* kernels_##TAG##_##NU##_##ND() {                                    \
+    static const KernelSetT<R> ks =                                                       \
+        merge_parts<R>({kparts_##TAG##_##NU##_##ND##_0(), kparts_##TAG##_##NU##_##ND##_1(), \
+                        kparts_##TAG##_##NU##_##ND##_2(), kparts_##TAG##_##NU##_##ND##_r()}); \
+    return &ks;                                                                           \
+  }
+#define MOLE_DECL(NU, ND)               \
+  MOLE_DECL_PARTS(NU, ND, double, f64) \
+  MOLE_DECL_PARTS(NU, ND, float, f32)
 MOLE_DECL(1, 0)
 MOLE_DECL(1, 1)
 MOLE_DECL(2, 1)

@@ -72,19 +72,32 @@ typename KernelSetT<R>::Dmc maybe_dmc() {
   else return nullptr;
 }
 
-// SR2: compile the exact two-parameter SR kernels (the H2 optimisation);
-// SR8: the eight-wide SR kernels; DRIFT: drift-diffusion VMC and DMC.
+// The VMC launchers of one SR width: [drift][e-n Jastrow]; ON = false leaves
+// them NULL, DRIFT = false the drift-diffusion ones.
 #define MOLE_VMC_EN(NU, ND, R, PM, ON, DRIFT)                                                             \
   {{maybe_vmc<NU, ND, R, PM, false, false, ON>(), maybe_vmc<NU, ND, R, PM, false, true, ON>()},          \
    {maybe_vmc<NU, ND, R, PM, true, false, (ON && DRIFT)>(), maybe_vmc<NU, ND, R, PM, true, true, (ON && DRIFT)>()}}
-#define MOLE_INSTANTIATE(NU, ND, R, TAG, SR2, SR8, DRIFT)                                                 \
-  const KernelSetT<R>* kernels_##TAG##_##NU##_##ND() {                                                   \
-    static const KernelSetT<R> ks = {                                                                    \
-        {MOLE_VMC_EN(NU, ND, R, 0, true, DRIFT), MOLE_VMC_EN(NU, ND, R, 2, SR2, DRIFT),                   \
-         MOLE_VMC_EN(NU, ND, R, 8, SR8, DRIFT)},                                                         \
-        {launch_eval<NU, ND, R, false>, launch_eval<NU, ND, R, true>},                                   \
-        {maybe_dmc<NU, ND, R, false, DRIFT>(), maybe_dmc<NU, ND, R, true, DRIFT>()}};                    \
-    return &ks;                                                                                          \
+// Slices of a family's kernel set, one translation unit each so that the
+// build compiles them in parallel; capi.cu merges them (kernel_set64/32).
+// Slot SLOT holds the VMC launchers with PM SR accumulators (drift and
+// non-drift, without and with the e-n term); the rest slice holds the
+// evaluation and DMC launchers.
+#define MOLE_PART_VMC(NU, ND, R, TAG, SLOT, PM)                                                     \
+  KernelSetT<R> kparts_##TAG##_##NU##_##ND##_##SLOT() {                                            \
+    KernelSetT<R> k{};                                                                             \
+    const typename KernelSetT<R>::Vmc v[2][2] = MOLE_VMC_EN(NU, ND, R, PM, true, true);              \
+    for (int d = 0; d < 2; ++d)                                                                    \
+      for (int e = 0; e < 2; ++e) k.vmc[SLOT][d][e] = v[d][e];                                     \
+    return k;                                                                                      \
+  }
+#define MOLE_PART_REST(NU, ND, R, TAG)                                                              \
+  KernelSetT<R> kparts_##TAG##_##NU##_##ND##_r() {                                                 \
+    KernelSetT<R> k{};                                                                             \
+    k.eval[0] = launch_eval<NU, ND, R, false>;                                                     \
+    k.eval[1] = launch_eval<NU, ND, R, true>;                                                      \
+    k.dmc[0] = launch_dmc<NU, ND, R, false>;                                                       \
+    k.dmc[1] = launch_dmc<NU, ND, R, true>;                                                        \
+    return k;                                                                                      \
   }
 
 // Double-float (FP64-accurate) kernels: box and Gaussian VMC and evaluation;

@@ -1,0 +1,6 @@
+// Mixed-precision VMC launchers without SR sums, spin blocks of 1 up and 0 down electrons.
+#include "dispatch.cuh"
+
+namespace mole {
+MOLE_PART_VMC(1, 0, float, f32, 0, 0)
+}  // namespace mole

@@ -1,0 +1,6 @@
+// Mixed-precision evaluation and DMC launchers, spin blocks of 1 up and 1 down electrons.
+#include "dispatch.cuh"
+
+namespace mole {
+MOLE_PART_REST(1, 1, float, f32)
+}  // namespace mole

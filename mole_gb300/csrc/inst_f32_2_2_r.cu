@@ -1,0 +1,6 @@
+// Mixed-precision evaluation and DMC launchers, spin blocks of 2 up and 2 down electrons.
+#include "dispatch.cuh"
+
+namespace mole {
+MOLE_PART_REST(2, 2, float, f32)
+}  // namespace mole
