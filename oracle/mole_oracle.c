@@ -1,7 +1,7 @@
 /*
  * mole_oracle.c -- CPU FP64 oracle for the mole walker hot path.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the GPU path, never shipped or
+ * TEST INFRASTRUCTURE ONLY: the reference the GPU path is compared with, never shipped or
  * called by it. Reference citations are file:line inside Jvanrhijn/mole.
  *
  * Independence from the GPU path: determinants here are formed densely and

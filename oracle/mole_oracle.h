@@ -3,7 +3,8 @@
  *
  * TEST INFRASTRUCTURE ONLY. Nothing in the product (mole_gb300/, include/)
  * links or calls this code; only tests/, __graft_entry__.smoke() and the CPU
- * baseline leg of bench.py use it, and only as the checker.
+ * baseline leg of bench.py use it, and only as the reference the GPU results
+ * are compared with.
  *
  * It restates the reference's algorithm (Jvanrhijn/mole, Rust) in plain C:
  *   - Metropolis box / diffuse moves        src/metropolis/src/metrop.rs:60-82, 150-198

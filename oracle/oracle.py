@@ -1,7 +1,8 @@
 """ctypes front end of the CPU FP64 oracle (oracle/mole_oracle.c).
 
 TEST INFRASTRUCTURE ONLY. Imported by tests/, __graft_entry__.smoke() and the
-CPU-baseline leg of bench.py, and only as the checker; the product package
+CPU-baseline leg of bench.py, and only as the reference the GPU results are
+compared with; the product package
 never imports it. It accepts any object with the attributes of
 ``mole_gb300.system.System`` (duck-typed, so the oracle carries no product
 code).
