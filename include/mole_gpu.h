@@ -173,8 +173,9 @@ int mole_ctx_df64_reruns(mole_ctx* ctx, int64_t* reruns);
  * 3 = double-float reciprocal, 4 = double-float x / (1 + x^2), 5 = x rounded
  * to float and widened by the integer-built conversion, 6 = x narrowed to
  * float toward zero by the integer-built conversion, 7 = the same for
- * magnitudes below FP32's largest (positions). Results go to the host array
- * y. */
+ * magnitudes below FP32's largest (positions), 8 = the FP64 reciprocal and
+ * 9 = the FP64 reciprocal square root of the native FP64 kernels. Results go
+ * to the host array y. */
 int mole_math_check(mole_ctx* ctx, int32_t fn, const double* x, int64_t n, double* y);
 /* Device FP64 and FP32 FMA peaks measured by a microbenchmark (GFLOP/s). */
 int mole_probe_peaks(mole_ctx* ctx, double* fp64_gflops, double* fp32_gflops);

@@ -87,7 +87,8 @@ class Context:
         """The library's device arithmetic on x (0: FP64 exp of the native kernels,
         1-4: double-float exp, rsqrt, reciprocal, x / (1 + x^2); 5, 6: the
         integer-built float -> double and double -> float (toward zero)
-        conversions; 7: the latter for magnitudes below FP32's largest)."""
+        conversions; 7: the latter for magnitudes below FP32's largest; 8, 9: the
+        FP64 reciprocal and reciprocal square root of the native kernels)."""
         x = np.ascontiguousarray(x, dtype=np.float64)
         y = np.empty_like(x)
         check(self.lib.mole_math_check(self.h, fn, dptr(x), x.size, dptr(y)))

@@ -266,7 +266,13 @@ __device__ __forceinline__ int batch_move(const SysParams<R>& sp, const BatchWal
   R uacc;
   uint32_t ubits;
   float z[3];
-  if constexpr (MOVE == kMoveBox) {
+  double v64[3];  // FP64 form: the unit proposal (u - 1/2 exactly, or the FP32 normal)
+  if constexpr (MOVE == kMoveBox && F64) {
+    v64[0] = u01_centered(ra.x);
+    v64[1] = u01_centered(ra.y);
+    v64[2] = u01_centered(ra.z);
+    ubits = ra.w;
+  } else if constexpr (MOVE == kMoveBox) {
     dx[0] = step * (u01<R>(ra.x) - (R)0.5);
     dx[1] = step * (u01<R>(ra.y) - (R)0.5);
     dx[2] = step * (u01<R>(ra.z) - (R)0.5);
@@ -280,7 +286,10 @@ __device__ __forceinline__ int batch_move(const SysParams<R>& sp, const BatchWal
     uacc = u01<R>(rb.x);
     ubits = rb.x;
 #pragma unroll
-    for (int c = 0; c < 3; ++c) dx[c] = step * from_f<R>(z[c]);
+    for (int c = 0; c < 3; ++c) {
+      if constexpr (F64) v64[c] = f2d(z[c]);
+      else dx[c] = step * from_f<R>(z[c]);
+    }
   }
   const R ro[3] = {wk.xr(e, 0), wk.xr(e, 1), wk.xr(e, 2)};
   R rn[3];
@@ -288,7 +297,7 @@ __device__ __forceinline__ int batch_move(const SysParams<R>& sp, const BatchWal
   if constexpr (F64) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      xn[c] = ro[c] + (double)dx[c];
+      xn[c] = fma((double)step, v64[c], (double)ro[c]);  // x + step v rounded once
       rn[c] = xn[c];
     }
   } else {

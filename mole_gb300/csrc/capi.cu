@@ -145,6 +145,8 @@ void fill_params(const mole_system& s, SysParams<R>& sp) {
     for (int k = 0; k < s.n_up; ++k) sp.coef[0][k][j] = (R)s.coef_up[(size_t)k * s.n_basis + b];
     for (int k = 0; k < s.n_dn; ++k) sp.coef[1][k][j] = (R)s.coef_dn[(size_t)k * s.n_basis + b];
   }
+  sp.all_sto1s = 1;
+  for (int j = 0; j < s.n_basis; ++j) sp.all_sto1s = sp.all_sto1s && sp.b_kind[j] == kSto1s;
   sp.n_exp = s.n_exp;
   sp.off_ee = s.n_exp;
   sp.off_en = sp.off_ee + (s.ee_on ? 1 + s.ee_npoly : 0);
@@ -155,8 +157,10 @@ void fill_params(const mole_system& s, SysParams<R>& sp) {
   sp.ee_kappa = (R)s.ee_kappa;
   sp.cusp_anti = (R)s.cusp_anti;
   sp.cusp_para = (R)s.cusp_para;
+  sp.ee_scaled = s.ee_kappa > 0.0 ? 1 : 0;
   if (s.ee_on) {
     sp.ee_b = (R)s.theta[sp.off_ee];
+    sp.ee_m2b = (R)(-2.0 * s.theta[sp.off_ee]);
     for (int p = 0; p < s.ee_npoly; ++p) sp.ee_poly[p] = (R)s.theta[sp.off_ee + 1 + p];
   }
   sp.en_on = s.en_on;
@@ -365,7 +369,7 @@ int mole_ctx_kernel_time(mole_ctx* c, int32_t kernel, double* total_ms, int64_t*
 
 int mole_math_check(mole_ctx* c, int32_t fn, const double* x, int64_t n, double* y) {
   cudaGetLastError();
-  if (!c || !x || !y || n < 0 || fn < 0 || fn > 7) return fail(MOLE_ERR_INVALID_ARG, "bad argument");
+  if (!c || !x || !y || n < 0 || fn < 0 || fn > 9) return fail(MOLE_ERR_INVALID_ARG, "bad argument");
   CUDA_TRY(c->scratch.reserve((size_t)2 * std::max<int64_t>(n, 1)));
   double* dx = c->scratch.p;
   double* dy = dx + n;

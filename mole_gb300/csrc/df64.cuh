@@ -16,18 +16,16 @@
 //   addition      the "sloppy" double-double add of Hida, Li and Bailey (QD, 2001)
 //   reciprocal, reciprocal square root: one Newton correction of the FP32
 //                 hardware approximation, with the residual formed exactly
-//   exp           reduction by ln2/64 (three-part constant), 64-entry table of
-//                 2^(j/64), degree-5 polynomial on |r| <= ln2/128
+//   exp           Tang's table-driven method (P. T. P. Tang, ACM TOMS 15(2),
+//                 1989): reduction by ln2/64 (three-part constant), 64-entry
+//                 table of 2^(j/64), degree-5 polynomial on |r| <= ln2/128;
+//                 the constants and tables are derived from exact arithmetic
+//                 by mole_gb300/gen_exp_constants.py (checked by the tests)
 // Every FP32 operation in the transformations uses the _rn intrinsics so that
 // the compiler cannot contract or reassociate them.
 //
-// exp64 is an FP64 exponential for the native FP64 kernels built on the same
-// pieces: FP64 argument reduction, e^r - 1 in double-float (small enough that
-// 2^-47 relative is below half an FP64 ulp of the result), one FP64 FMA to
-// finish: five FP64-pipe instructions against the library's fifteen (counted
-// with smsp__inst_executed_pipe_fp64 in a microbenchmark), its float <-> double
-// conversions done with integer operations (f2d, d2f_rz below), since a
-// hardware conversion takes an FP64-pipe slot like a DADD.
+// fp64.cuh builds the native FP64 kernels' reciprocal, reciprocal square root
+// and exponential on the same pieces.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -282,36 +280,6 @@ __device__ __forceinline__ df64 df_exp(df64 x) {
   return df_scale(v, __int_as_float((k + 127) << 23));
 }
 
-// e^x in FP64 to about 1.5 ulp. x = n ln2/64 + r, n = rint(64 x / ln2) from the
-// FP32 value of x, r = x - n L1 - n L2 in FP64 (L1: 37-bit head of ln2/64, so
-// n L1 is exact for |n| < 2^16); q = e^r - 1 = r + r^2/2 + r^3/6 in
-// double-float plus r^4/24 + r^5/120 + r^6/720 in FP32 (|q| < 0.0056, error
-// below 2^-54); e^x = 2^(n >> 6) (T + T q), T = 2^((n & 63)/64). Outside
-// |x| < 700 (overflow, subnormal results) the library exp.
-__device__ __forceinline__ double exp64(double x) {
-  const float xf = d2f_rz(x);
-  if (!(fabsf(xf) < 700.f)) return exp(x);
-  constexpr double kL1 = 0x1.62e42fefa0000p-7;
-  constexpr double kL2 = 0x1.cf79abc9e3b3ap-46;
-  const float n = rintf(__fmul_rn(xf, 92.33248261689366f));
-  const double nd = f2d(n);
-  double r = fma(-nd, kL1, x);
-  r = fma(-nd, kL2, r);
-  // r as a double-float: its top 24 bits, then the (exact) remainder's
-  const float rh = d2f_rz(r);
-  const df64 rd(rh, d2f_rz(r - f2d(rh)));
-  float t = __fmaf_rn(rh, 1.0f / 720.0f, 1.0f / 120.0f);
-  t = __fmaf_rn(rh, t, 1.0f / 24.0f);
-  const df64 a = df_mul(rd, t) + df64(0x1.555556p-3f, -0x1.555556p-28f);  // 1/6 + r t
-  const df64 b = rd * a + df64(0.5f);
-  const df64 q = rd + rd * (rd * b);
-  const int ni = (int)n;
-  const double T = __ldg(&kExp2Tab64[ni & 63]);
-  const double v = fma(T, f2d(q.h) + f2d(q.l), T);
-  // scale by 2^(n >> 6) in the exponent field (v is in [1, 2.1), the result normal)
-  return __hiloint2double(__double2hiint(v) + (ni >> 6) * (1 << 20), __double2loint(v));
-}
-
 __device__ __forceinline__ df64& operator+=(df64& a, df64 b) { return a = a + b; }
 __device__ __forceinline__ df64& operator-=(df64& a, df64 b) { return a = a - b; }
 __device__ __forceinline__ df64& operator*=(df64& a, df64 b) { return a = a * b; }
@@ -339,9 +307,18 @@ __device__ __forceinline__ bool is_zero(double x) { return x == 0.0; }
 __device__ __forceinline__ bool is_pos(double x) { return x > 0.0; }
 __device__ __forceinline__ bool is_pos(df64 x) { return x.h > 0.f; }
 __device__ __forceinline__ bool is_zero(df64 x) { return x.h == 0.f; }
-__device__ __forceinline__ double recip(double x) { return 1.0 / x; }
 __device__ __forceinline__ df64 recip(df64 x) { return df_rcp(x); }
 __device__ __forceinline__ double twice(double x) { return 2.0 * x; }
+// The start of a sum: -0 for double (-0 + a = a for every a, so the first
+// addition folds away), zero for df64.
+template <class F>
+__device__ __forceinline__ F acc_zero() {
+  return F(0);
+}
+template <>
+__device__ __forceinline__ double acc_zero<double>() {
+  return -0.0;
+}
 __device__ __forceinline__ df64 twice(df64 x) { return df64(__fmul_rn(x.h, 2.f), __fmul_rn(x.l, 2.f)); }
 
 }  // namespace mole

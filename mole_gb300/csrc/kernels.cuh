@@ -103,9 +103,8 @@ __device__ __forceinline__ void vmc_body(const SysParams<R>& sp, const VmcArgs& 
     F O[PM > 0 ? PM : 1];
     const F E = wk.local_energy(sp, O, nullptr, nullptr);
     const int k = it - a.n_eq;
-    sE += E;
     sE2 += E * E;
-    bsum += E;
+    bsum += E;  // added to sE at every block end and after the last sweep
     if constexpr (PM > 0) {
 #pragma unroll
       for (int p = 0; p < PM; ++p) {
@@ -125,9 +124,11 @@ __device__ __forceinline__ void vmc_body(const SysParams<R>& sp, const VmcArgs& 
       double v[1] = {active ? bs : 0.0};
       block_sum<1>(v, red);
       if (threadIdx.x == 0) a.tb_partials[(size_t)blockIdx.x * (a.n_steps / a.block_size) + k / a.block_size] = v[0];
+      sE += bsum;
       bsum = F(0);
     }
   }
+  sE += bsum;
   const double dE = to_d(sE), dE2 = to_d(sE2);
   double acc[kNMom] = {(double)a.n_steps, dE, dE2, sB2, (double)(a.n_steps / a.block_size), (double)naccept,
                        (double)total * Wk::N};

@@ -1,9 +1,9 @@
 // math_check.cu -- evaluates the library's own device arithmetic on arrays so
-// that tests can pin its accuracy: the FP64 exponential of the native FP64
-// kernels, the double-float exp, reciprocal square root and reciprocal of
-// the double-float kernels, and the integer-built float <-> double
-// conversions.
-#include "df64.cuh"
+// that tests can pin its accuracy: the FP64 exponential, reciprocal and
+// reciprocal square root of the native FP64 kernels, the double-float exp,
+// reciprocal square root and reciprocal of the double-float kernels, and the
+// integer-built float <-> double conversions.
+#include "fp64.cuh"
 
 namespace mole {
 
@@ -20,7 +20,9 @@ __global__ void math_check_kernel(int fn, const double* x, int64_t n, double* y)
     case 4: r = (double)(df64(v) / df64(1.0 + v * v)); break;
     case 5: r = f2d(__double2float_rn(v)); break;
     case 6: r = (double)d2f_rz(v); break;
-    default: r = (double)d2f_rz_small(v); break;
+    case 7: r = (double)d2f_rz_small(v); break;
+    case 8: r = rcp64(v); break;
+    default: r = rsqrt64(v); break;
   }
   y[i] = r;
 }

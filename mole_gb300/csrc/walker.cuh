@@ -20,6 +20,7 @@
 
 #include "common.cuh"
 #include "df64.cuh"
+#include "fp64.cuh"
 #include "nn.cuh"
 #include "normal.cuh"
 
@@ -33,12 +34,15 @@ struct SysParams {
   int nuc_b0[kMaxNuc + 1];  // basis functions of nucleus I are [nuc_b0[I], nuc_b0[I+1])
   int b_kind[kMaxBasis];
   int b_exp[kMaxBasis];  // exponent parameter index of basis function b
+  int all_sto1s;         // every basis function is a 1s STO
   R nuc_pos[kMaxNuc * 3];
   R nuc_z[kMaxNuc];
   R b_zeta[kMaxBasis];
   R coef[2][kMaxSpin][kMaxBasis];  // [spin][orbital][basis]
   int ee_on, ee_npoly;
+  int ee_scaled;  // ee_kappa > 0: the Pade term of the scaled distance (1 - e^-kappa r) / kappa
   R ee_kappa, cusp_anti, cusp_para, ee_b;
+  R ee_m2b;  // -2 ee_b
   R ee_poly[kMaxPoly];
   int en_on;
   R en_a;
@@ -57,7 +61,7 @@ template <class R>
 __device__ __forceinline__ R rsqrt_t(R x);
 template <>
 __device__ __forceinline__ double rsqrt_t<double>(double x) {
-  return rsqrt(x);
+  return rsqrt64(x);
 }
 template <>
 __device__ __forceinline__ float rsqrt_t<float>(float x) {
@@ -80,6 +84,28 @@ __device__ __forceinline__ float exp_t<float>(float x) {
 template <>
 __device__ __forceinline__ df64 exp_t<df64>(df64 x) {
   return df_exp(x);
+}
+// e^(-z r): in FP64 the product is fused into the argument reduction.
+template <class R>
+__device__ __forceinline__ R expm_t(R z, R r) {
+  return exp_t<R>(-(z * r));
+}
+template <>
+__device__ __forceinline__ double expm_t<double>(double z, double r) {
+  return expab64(-z, r);
+}
+// 1 / x: two FP64 instructions in FP64, IEEE division in FP32, Newton in df64.
+template <class R>
+__device__ __forceinline__ R recip_t(R x) {
+  return (R)1 / x;
+}
+template <>
+__device__ __forceinline__ double recip_t<double>(double x) {
+  return rcp64(x);
+}
+template <>
+__device__ __forceinline__ df64 recip_t<df64>(df64 x) {
+  return df_rcp(x);
 }
 
 // One electron's orbitals of its spin block (value, gradient, Laplacian),
@@ -129,70 +155,114 @@ __device__ __forceinline__ void one_body(const SysParams<R>& sp, int spin, const
     const R inv = rsqrt_t<R>(r2);
     const R rr = r2 * inv;
     o.ven -= sp.nuc_z[I] * inv;
-    const int b1 = sp.nuc_b0[I + 1];
-    #pragma unroll 1
-    for (int b = sp.nuc_b0[I]; b < b1; ++b) {
-      const int kind = sp.b_kind[b];
+    // one basis function b of compile-time kind K (K < 0: read at run time);
+    // a system whose basis is all 1s STOs takes a loop without the kind
+    // branches, which the compiler would otherwise turn into predicated FP64
+    // instructions of every kind
+    auto basis = [&](auto kc, int b) {
+      constexpr int K = decltype(kc)::value;
+      const int kind = K >= 0 ? K : sp.b_kind[b];
       const R z = sp.b_zeta[b];
-      R chi, g0, g1, g2, l, rad;
-      if (kind == kGto1s) {
-        const R e = exp_t<R>(-z * r2);
-        const R f = (R)-2 * z * e;
+      const bool gto = kind == kGto1s;
+      const R rad = gto ? r2 : rr;
+      R e = expm_t<R>(z, rad);
+      // with one orbital the coefficient is folded into e: every basis value
+      // below is linear in e
+      if constexpr (n == 1) e *= sp.coef[spin][0][b];
+      // chi, its gradient fr d (+ e along one axis for 2p), its Laplacian
+      // la lb, d chi / dz = -rad chi
+      R chi, fr, la, lb;
+      int ax = -1;
+      if (gto) {
         chi = e;
-        g0 = f * d0; g1 = f * d1; g2 = f * d2;
-        l = e * ((R)4 * z * z * r2 - (R)6 * z);
-        rad = r2;
+        fr = (R)-2 * z * e;
+        la = fr;
+        lb = (R)3 - z * r2 - z * r2;  // lap = e (4 z^2 r^2 - 6 z)
+      } else if (kind == kSto1s) {
+        chi = e;
+        la = z * e;
+        fr = -la * inv;
+        lb = z - (R)2 * inv;  // lap = z e (z - 2 / r)
+      } else if (kind == kSto2s) {
+        chi = rr * e;
+        fr = e * ((R)1 - z * rr) * inv;
+        la = e;
+        lb = z * z * rr - (R)4 * z + (R)2 * inv;
       } else {
-        const R e = exp_t<R>(-z * rr);
-        rad = rr;
-        if (kind == kSto1s) {
-          const R f = -z * e * inv;
-          chi = e;
-          g0 = f * d0; g1 = f * d1; g2 = f * d2;
-          l = e * (z * z - (R)2 * z * inv);
-        } else if (kind == kSto2s) {
-          const R f = e * ((R)1 - z * rr) * inv;
-          chi = rr * e;
-          g0 = f * d0; g1 = f * d1; g2 = f * d2;
-          l = e * (z * z * rr - (R)4 * z + (R)2 * inv);
-        } else {
-          const R da = kind == kSto2px ? d0 : (kind == kSto2py ? d1 : d2);
-          const R f = -z * da * e * inv;
-          chi = da * e;
-          g0 = f * d0; g1 = f * d1; g2 = f * d2;
-          if (kind == kSto2px) g0 += e;
-          else if (kind == kSto2py) g1 += e;
-          else g2 += e;
-          l = da * e * (z * z - (R)4 * z * inv);
-        }
+        ax = kind - kSto2px;
+        const R da = ax == 0 ? d0 : (ax == 1 ? d1 : d2);
+        chi = da * e;
+        la = z * chi;
+        fr = -la * inv;
+        lb = z - (R)4 * inv;  // lap = z chi (z - 4 / r)
       }
-      const R dzb = -rad * chi;
       const int ix = sp.b_exp[b];
-#pragma unroll
-      for (int k = 0; k < n; ++k) {
-        const R c = sp.coef[spin][k][b];
-        o.val[k] += c * chi;
-        o.grad[k][0] += c * g0;
-        o.grad[k][1] += c * g1;
-        o.grad[k][2] += c * g2;
-        o.lap[k] += c * l;
+      if constexpr (n == 1) {
+        o.val[0] += chi;
+        if (ax < 0) {
+          o.grad[0][0] += fr * d0;
+          o.grad[0][1] += fr * d1;
+          o.grad[0][2] += fr * d2;
+        } else {  // 2p: + e along its axis
+          o.grad[0][0] += fr * d0 + (ax == 0 ? e : (R)0);
+          o.grad[0][1] += fr * d1 + (ax == 1 ? e : (R)0);
+          o.grad[0][2] += fr * d2 + (ax == 2 ? e : (R)0);
+        }
+        o.lap[0] += la * lb;
         if constexpr (NZ > 0) {
 #pragma unroll
           for (int p = 0; p < NZ; ++p)
-            if (p == ix) o.dz[k][p] += c * dzb;
+            if (p == ix) o.dz[0][p] -= rad * chi;
+        }
+      } else {
+        const R l = la * lb;
+        const R dzb = -rad * chi;
+#pragma unroll
+        for (int k = 0; k < n; ++k) {
+          const R c = sp.coef[spin][k][b];
+          const R cf = c * fr;
+          o.val[k] += c * chi;
+          if (ax < 0) {
+            o.grad[k][0] += cf * d0;
+            o.grad[k][1] += cf * d1;
+            o.grad[k][2] += cf * d2;
+          } else {  // 2p: + c e along its axis
+            const R ce = c * e;
+            o.grad[k][0] += cf * d0 + (ax == 0 ? ce : (R)0);
+            o.grad[k][1] += cf * d1 + (ax == 1 ? ce : (R)0);
+            o.grad[k][2] += cf * d2 + (ax == 2 ? ce : (R)0);
+          }
+          o.lap[k] += c * l;
+          if constexpr (NZ > 0) {
+#pragma unroll
+            for (int p = 0; p < NZ; ++p)
+              if (p == ix) o.dz[k][p] += c * dzb;
+          }
         }
       }
+    };
+    const int b1 = sp.nuc_b0[I + 1];
+    if (sp.all_sto1s) {
+      #pragma unroll 1
+      for (int b = sp.nuc_b0[I]; b < b1; ++b) basis(std::integral_constant<int, kSto1s>{}, b);
+    } else {
+      #pragma unroll 1
+      for (int b = sp.nuc_b0[I]; b < b1; ++b) basis(std::integral_constant<int, -1>{}, b);
     }
     if (EN) {
+      // Pade e-n term A r / (1 + a r): value, gradient A q^2 d / r,
+      // Laplacian 2 A q^2 (1/r - a q), d/da -A r^2 q^2, q = 1 / (1 + a r)
       const R A = sp.en_coef[I];
-      const R q = (R)1 / ((R)1 + sp.en_a * rr);
-      const R du = A * q * q * inv;
-      o.jen += A * rr * q;
+      const R q = recip_t<R>((R)1 + sp.en_a * rr);
+      const R Aq = A * q;
+      const R Aq2 = Aq * q;
+      const R du = Aq2 * inv;
+      o.jen += Aq * rr;
       o.gjen[0] += du * d0;
       o.gjen[1] += du * d1;
       o.gjen[2] += du * d2;
-      o.ljen += (R)-2 * A * sp.en_a * q * q * q + (R)2 * A * q * q * inv;
-      if constexpr (NZ > 0) o.djen += -A * rr * rr * q * q;
+      o.ljen += (Aq2 + Aq2) * (inv - sp.en_a * q);
+      if constexpr (NZ > 0) o.djen -= Aq2 * rr * rr;
     }
     if constexpr (NN) {
       R y, y1, y2;
@@ -224,49 +294,78 @@ __device__ __forceinline__ void pair_vals(const SysParams<R>& sp, bool same, R d
   const R inv = rsqrt_t<R>(r2);
   const R r = r2 * inv;
   v.inv = inv;
-  v.u = 0;
-  v.f = 0;
-  v.l = 0;
   v.db = 0;
   v.rs = r;
+  R yn = 0, fn = 0, ln = 0;  // the e-e network's u, u'/r, u'' + 2u'/r
   if constexpr (NN) {
     R y, y1, y2;
     if constexpr (std::is_same<R, float>::value) nn_tab_eval(sp.nn_tab, same ? 0 : 1, r, y, y1, y2);
     else nn_jet<R>(nn->sh->net[0], r, same ? (R)1 : (R)0, nn->scr, nn->stride, y, y1, y2);
-    v.u = y;
-    v.f = y1 * inv;
-    v.l = y2 + (R)2 * v.f;
+    yn = y;
+    fn = y1 * inv;
+    ln = y2 + (R)2 * fn;
   }
-  if (!sp.ee_on) return;
+  if (!sp.ee_on) {
+    v.u = yn;
+    v.f = fn;
+    v.l = ln;
+    return;
+  }
   const R cusp = same ? sp.cusp_para : sp.cusp_anti;
-  R Rs = r, Rp = 1, Rpp = 0;
-  if (sp.ee_kappa > (R)0) {
+  R val, f, l;
+  if (sp.ee_scaled) {
+    // Pade term of the scaled distance Rs = (1 - e^-kappa r) / kappa
     const R e = exp_t<R>(-sp.ee_kappa * r);
-    Rs = ((R)1 - e) / sp.ee_kappa;
-    Rp = e;
-    Rpp = -sp.ee_kappa * e;
+    const R Rs = ((R)1 - e) / sp.ee_kappa;
+    const R Rp = e, Rpp = -sp.ee_kappa * e;
+    const R q = recip_t<R>((R)1 + sp.ee_b * Rs);
+    val = cusp * Rs * q;
+    R uR = cusp * q * q;
+    R uRR = (R)-2 * cusp * sp.ee_b * q * q * q;
+    if constexpr (PM > 0) v.db = -cusp * Rs * Rs * q * q;
+    R Rk = Rs, Rk2 = 1;  // R^(p-1), R^(p-2)
+    #pragma unroll 1
+    for (int i = 0; i < sp.ee_npoly; ++i) {
+      const R p = (R)(i + 2), c = sp.ee_poly[i];
+      val += c * Rk * Rs;
+      uR += p * c * Rk;
+      uRR += p * (p - (R)1) * c * Rk2;
+      Rk2 = Rk;
+      Rk *= Rs;
+    }
+    f = uR * Rp * inv;
+    l = uRR * Rp * Rp + uR * Rpp + (R)2 * f;
+    v.rs = Rs;
+  } else {
+    // u = c r q, u' = c q^2, u'' = -2 b c q^3, du/db = -c r^2 q^2, q = 1 / (1 + b r)
+    const R q = recip_t<R>((R)1 + sp.ee_b * r);
+    const R cq = cusp * q;
+    R uR = cq * q;
+    val = cq * r;
+    R uRR = sp.ee_m2b * q * uR;
+    if constexpr (PM > 0) v.db = -(r2 * uR);
+    R Rk = r, Rk2 = 1;  // r^(p-1), r^(p-2)
+    #pragma unroll 1
+    for (int i = 0; i < sp.ee_npoly; ++i) {
+      const R p = (R)(i + 2), c = sp.ee_poly[i];
+      val += c * Rk * r;
+      uR += p * c * Rk;
+      uRR += p * (p - (R)1) * c * Rk2;
+      Rk2 = Rk;
+      Rk *= r;
+    }
+    f = uR * inv;
+    l = uRR + (R)2 * f;
   }
-  const R q = (R)1 / ((R)1 + sp.ee_b * Rs);
-  R val = cusp * Rs * q;
-  R uR = cusp * q * q;
-  R uRR = (R)-2 * cusp * sp.ee_b * q * q * q;
-  if constexpr (PM > 0) v.db = -cusp * Rs * Rs * q * q;
-  R Rk = Rs, Rk2 = 1;  // R^(p-1), R^(p-2)
-  #pragma unroll 1
-  for (int i = 0; i < sp.ee_npoly; ++i) {
-    const R p = (R)(i + 2), c = sp.ee_poly[i];
-    val += c * Rk * Rs;
-    uR += p * c * Rk;
-    uRR += p * (p - (R)1) * c * Rk2;
-    Rk2 = Rk;
-    Rk *= Rs;
+  if constexpr (NN) {
+    v.u = yn + val;
+    v.f = fn + f;
+    v.l = ln + l;
+  } else {
+    v.u = val;
+    v.f = f;
+    v.l = l;
   }
-  const R du = uR * Rp;
-  const R f = du * inv;
-  v.rs = Rs;
-  v.u += val;
-  v.f += f;
-  v.l += uRR * Rp * Rp + uR * Rpp + (R)2 * f;
 }
 
 // The Metropolis test ratio^2 exp(x) > u, u = u01(ubits) >= 2^-33. With
@@ -278,6 +377,23 @@ __device__ __forceinline__ void pair_vals(const SysParams<R>& sp, bool same, R d
 // relative it decides exactly as the FP64 test. Everything else takes the
 // FP64 expression. Same decisions as FP64, the FP64 exp skipped in all but
 // borderline and extreme cases.
+// The FP64 expression of the test, as a call (a branch the compiler cannot
+// turn into predicated FP64 instructions on the screened path).
+static __device__ __noinline__ bool metropolis_fp64(double ratio, double x, uint32_t ubits) {
+  return ratio * ratio * exp(x) > u01<double>(ubits);
+}
+// The test for x = 2 dj, the doubling done in FP32 (exact) and, in the
+// borderline case, in FP64.
+__device__ __forceinline__ bool metropolis_accept_dj(double ratio, double dj, uint32_t ubits) {
+  const float rf = d2f_rz(ratio), xf = 2.f * d2f_rz(dj);
+  const float r2 = rf * rf;
+  if (fabsf(xf) < 80.f && r2 > 1e-30f && r2 < 1e30f) {
+    const float uf = u01<float>(ubits);
+    const float d = r2 * __expf(xf) - uf;
+    if (fabsf(d) > 1e-3f * uf) return d > 0.f;
+  }
+  return metropolis_fp64(ratio, dj + dj, ubits);
+}
 __device__ __forceinline__ bool metropolis_accept(double ratio, double x, uint32_t ubits) {
   const float rf = d2f_rz(ratio), xf = d2f_rz(x);  // truncated: no FP64-pipe conversion
   const float r2 = rf * rf;
@@ -608,9 +724,27 @@ struct Walker {
 
     const uint4 ra = draw4(seed, wid, t, 2u * e, kTagMove);
     F dx[3];
+    F xn[3];
     R uacc;
     uint32_t ubits;
-    if constexpr (MOVE == kMoveBox) {
+    // FP64 box and Gaussian moves: x + step v with one rounding (v = u - 1/2
+    // exactly, or the FP32 normal)
+    constexpr bool FMA_PROPOSAL = std::is_same<R, double>::value && !DRIFT;
+    if constexpr (FMA_PROPOSAL && MOVE == kMoveBox) {
+      xn[0] = fma(step, u01_centered(ra.x), x[e][0]);
+      xn[1] = fma(step, u01_centered(ra.y), x[e][1]);
+      xn[2] = fma(step, u01_centered(ra.z), x[e][2]);
+      ubits = ra.w;
+    } else if constexpr (FMA_PROPOSAL) {
+      float z0, z1, z2, z3;
+      repro_box_muller(ra.x, ra.y, z0, z1);
+      repro_box_muller(ra.z, ra.w, z2, z3);
+      const uint4 rb = draw4(seed, wid, t, 2u * e + 1u, kTagMove);
+      ubits = rb.x;
+      xn[0] = fma(step, f2d(z0), x[e][0]);
+      xn[1] = fma(step, f2d(z1), x[e][1]);
+      xn[2] = fma(step, f2d(z2), x[e][2]);
+    } else if constexpr (MOVE == kMoveBox) {
       dx[0] = (F)(step * (u01<R>(ra.x) - (R)0.5));
       dx[1] = (F)(step * (u01<R>(ra.y) - (R)0.5));
       dx[2] = (F)(step * (u01<R>(ra.z) - (R)0.5));
@@ -648,7 +782,11 @@ struct Walker {
         dx[2] = (double)step * vcur[e][2] + sq * (double)z2;
       }
     }
-    const F xn[3] = {x[e][0] + dx[0], x[e][1] + dx[1], x[e][2] + dx[2]};
+    if constexpr (!FMA_PROPOSAL) {
+      xn[0] = x[e][0] + dx[0];
+      xn[1] = x[e][1] + dx[1];
+      xn[2] = x[e][2] + dx[2];
+    }
     const R rn[3] = {to_r(xn[0]), to_r(xn[1]), to_r(xn[2])};  // as every other FP32 position
     OneBody<R, n, NZ> o;
     one_body<R, n, NZ, EN, NN>(sp, isup ? 0 : 1, rn, o, &nn);
@@ -656,8 +794,11 @@ struct Walker {
 #pragma unroll
     for (int k = 0; k < n; ++k) ratio += to_f(o.val[k]) * B[k * ld + i];
 
-    // new pair terms of electron e
-    R dJ = o.jen - jen[e];
+    // new pair terms of electron e (without one-body Jastrow terms the sum
+    // starts at -0, so that its first addition folds away)
+    R dJ;
+    if constexpr (EN || NN) dJ = o.jen - jen[e];
+    else dJ = acc_zero<R>();
     PairVals<R, PM> pv[N];
     static_for<0, N>([&](auto jc) {
       constexpr int j = decltype(jc)::value;
@@ -673,7 +814,7 @@ struct Walker {
     float bnf[F32 ? n * n : 1];
     if constexpr (!DRIFT) {
       if constexpr (std::is_same<R, double>::value) {
-        acc = metropolis_accept(ratio, 2.0 * dJ, ubits);
+        acc = metropolis_accept_dj(ratio, dJ, ubits);
       } else if constexpr (DF) {
         acc = metropolis_accept(ratio, twice(dJ), ubits);
       } else {
@@ -788,6 +929,12 @@ struct Walker {
         for (int k = 0; k < n * n; ++k) Bf[(k / n) * ld + (k % n)] = bnf[k];
       }
     } else {
+      if constexpr (n == 1) {
+        // a 1 x 1 block: the inverse is the reciprocal of the new orbital value
+        B[0] = recip(to_f(o.val[0]));
+        if constexpr (DF)
+          if (!(piv_mag(B[0]) < 0x1p96f)) oor = true;
+      } else {
       // Sherman-Morrison row update (FP64)
       F v[n], col[n];
 #pragma unroll
@@ -812,6 +959,7 @@ struct Walker {
           for (int j = 0; j < n; ++j) in = in && (piv_mag(B[k * ld + j]) < 0x1p96f);
         if (!in) oor = true;
       }
+      }
     }
     return 1;
   }
@@ -828,11 +976,24 @@ struct Walker {
   // for the first PM parameters. grad (optional) receives grad ln psi [N][3];
   // lapout receives sum_i lap_i psi / psi.
   __device__ F local_energy(const SP& sp, F (&O)[PMC], double* grad, double* lapout) const {
-    F lap = F(0), V = F(0);
+    // pair gradient vectors u'(r)/r (x_i - x_j), i < j, formed once: electron
+    // i's Jastrow gradient takes +, electron j's takes -
+    R gp[NPm][3];
+    static_for<0, N>([&](auto ic) {
+      constexpr int i = decltype(ic)::value;
+      static_for<i + 1, N>([&](auto jc) {
+        constexpr int j = decltype(jc)::value;
+        constexpr int p = pidx(i, j);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) gp[p][c] = pf[p] * to_r(x[i][c] - x[j][c]);
+      });
+    });
+    // sums start at -0 so that the first addition folds away (-0 + a = a)
+    F lap = acc_zero<F>(), V = acc_zero<F>();
     if constexpr (PM > 0)
 #pragma unroll
-      for (int p = 0; p < PM; ++p) O[p] = F(0);
-    F djs = F(0);
+      for (int p = 0; p < PM; ++p) O[p] = acc_zero<F>();
+    F djs = acc_zero<F>();
     static_for<0, N>([&](auto ec) {
       constexpr int e = decltype(ec)::value;
       constexpr bool isup = e < NU;
@@ -844,12 +1005,32 @@ struct Walker {
       det_grad<e>(gD);
 #pragma unroll
       for (int k = 0; k < n; ++k) lD += to_f(ol[e][k]) * B[k * ld + i];
-      R gJ[3];
-      jas_grad<e>(gJ);
-      R lJ = ljen[e];
+      // Jastrow gradient and Laplacian at electron e from the caches
+      R gJ[3], lJ;
+      if constexpr (EN) {
+        gJ[0] = gjen[e][0];
+        gJ[1] = gjen[e][1];
+        gJ[2] = gjen[e][2];
+        lJ = ljen[e];
+      } else {
+        gJ[0] = gJ[1] = gJ[2] = 0;  // replaced by the first pair term when there is one
+        lJ = 0;
+      }
+      static_for<0, N>([&](auto mc) {
+        constexpr int m = decltype(mc)::value;
+        if constexpr (m != e) {
+          constexpr int p = pidx(e, m);
+          constexpr bool first = !EN && m == (e == 0 ? 1 : 0);
 #pragma unroll
-      for (int m = 0; m < N; ++m)
-        if (m != e) lJ += pl[pidx(e, m)];
+          for (int c = 0; c < 3; ++c) {
+            const R g = e < m ? gp[p][c] : -gp[p][c];
+            if constexpr (first) gJ[c] = g;
+            else gJ[c] += g;
+          }
+          if constexpr (first) lJ = pl[p];
+          else lJ += pl[p];
+        }
+      });
       F dot = F(0), gj2 = F(0);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
@@ -859,17 +1040,17 @@ struct Walker {
         if (grad) grad[3 * e + c] = to_d(gD[c] + gj);
       }
       lap += lD + to_f(lJ) + twice(dot) + gj2;
-      if (sp.pot_kind == 0) V += to_f(ven[e]);
-      else V += to_f(sp.half_omega2) * (x[e][0] * x[e][0] + x[e][1] * x[e][1] + x[e][2] * x[e][2]);
+      V += to_f(ven[e]);  // -sum_I Z_I / r_iI (zero charges in the harmonic well)
       if constexpr (PM > 0) {
+        // exponent derivatives: the first NZ slots
 #pragma unroll
-        for (int p = 0; p < PM; ++p) {
+        for (int p = 0; p < NZ; ++p) {
           F s = F(0);
 #pragma unroll
           for (int k = 0; k < n; ++k) s += to_f(odz[e][k][p]) * B[k * ld + i];
           O[p] += s;
         }
-        djs += to_f(djen[e]);
+        if constexpr (EN) djs += to_f(djen[e]);
       }
     });
     if (sp.pot_kind == 0) {
@@ -878,17 +1059,29 @@ struct Walker {
       if constexpr (DF) V += sp.vnn_r;
       else V += sp.vnn;
     }
-    if constexpr (PM > 0) {
-      F dudb = F(0), dpoly[kMaxPoly] = {F(0), F(0), F(0), F(0)};
+    // the harmonic well (pot_kind 1) as a loop of at most one trip: a branch
+    // rather than FP64 instructions predicated off in every Coulomb system
+    #pragma unroll 1
+    for (int h = 0; h < sp.pot_kind; ++h)
 #pragma unroll
-      for (int p = 0; p < NP; ++p) {
-        dudb += to_f(pdb[p]);
+      for (int e = 0; e < N; ++e)
+        V += to_f(sp.half_omega2) * (x[e][0] * x[e][0] + x[e][1] * x[e][1] + x[e][2] * x[e][2]);
+    if constexpr (PM > 0) {
+      F dudb = acc_zero<F>();
+      F dpoly[kMaxPoly] = {acc_zero<F>(), acc_zero<F>(), acc_zero<F>(), acc_zero<F>()};
+#pragma unroll
+      for (int p = 0; p < NP; ++p) dudb += to_f(pdb[p]);
+      if (sp.ee_npoly > 0) {
         // d u / d b_(q+3) = R^(q+2)
-        F rk = to_f(prs[p]) * to_f(prs[p]);
-        #pragma unroll 1
-        for (int q = 0; q < sp.ee_npoly; ++q) {
-          dpoly[q] += rk;
-          rk *= to_f(prs[p]);
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          const F rs = to_f(prs[p]);
+          F rk = rs * rs;
+#pragma unroll
+          for (int q = 0; q < kMaxPoly; ++q) {
+            if (q < sp.ee_npoly) dpoly[q] += rk;
+            rk *= rs;
+          }
         }
       }
 #pragma unroll

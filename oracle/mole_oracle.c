@@ -634,10 +634,11 @@ static int move_electron(const orc_system* s, const double* th, int N, double* p
   draw4(seed, walker, t, (uint32_t)(2 * e), TAG_MOVE, ua);
   double prop[ORC_MAX_ELEC * 3];
   memcpy(prop, pos, sizeof(double) * 3 * N);
-  double dx[3];
+  double dx[3] = {0.0, 0.0, 0.0};
   double uacc;
+  /* box and Gaussian moves: x + step v rounded once (fma; u - 1/2 is exact) */
   if (move == ORC_MOVE_BOX) {
-    for (int k = 0; k < 3; ++k) dx[k] = step * (u01(ua[k]) - 0.5);
+    for (int k = 0; k < 3; ++k) prop[3 * e + k] = fma(step, u01(ua[k]) - 0.5, prop[3 * e + k]);
     uacc = u01(ua[3]);
   } else {
     float z[4];
@@ -646,13 +647,13 @@ static int move_electron(const orc_system* s, const double* th, int N, double* p
     draw4(seed, walker, t, (uint32_t)(2 * e + 1), TAG_MOVE, ub);
     uacc = u01(ub[0]);
     if (move == ORC_MOVE_GAUSS) {
-      for (int k = 0; k < 3; ++k) dx[k] = step * (double)z[k];
+      for (int k = 0; k < 3; ++k) prop[3 * e + k] = fma(step, (double)z[k], prop[3 * e + k]);
     } else {
       double sq = sqrt(step);
       for (int k = 0; k < 3; ++k) dx[k] = step * cur->grad[3 * e + k] + sq * (double)z[k];
+      for (int k = 0; k < 3; ++k) prop[3 * e + k] += dx[k];
     }
   }
-  for (int k = 0; k < 3; ++k) prop[3 * e + k] += dx[k];
   wstate nw;
   if (eval_state(s, th, prop, &nw) != 0) return 0;
   double logA = 2.0 * (nw.lnpsi - cur->lnpsi);

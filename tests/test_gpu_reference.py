@@ -60,6 +60,42 @@ def test_steepest_descent_moves_downhill(ctx):
     assert energies[-1] < energies[0] - 0.1
 
 
+class _Grad:
+    def __init__(self, g):
+        self.g = np.asarray(g, dtype=np.float64)
+
+    def energy_gradient(self):
+        return self.g.copy()
+
+
+@pytest.mark.parametrize("name", ["momentum", "nesterov", "lbfgs"])
+def test_host_optimizers_through_vmc_runner(ctx, name):
+    """MomentumDescent, NesterovMomentum and OnlineLbfgs (optimizers.rs:45-192)
+    driving VmcRunner on the harmonic well: every update the runner applies is
+    the optimizer's rule on the device-reduced gradient (a fresh optimizer fed
+    the recorded gradients reproduces the parameter trajectory), the momentum
+    forms lower the energy from psi's exponent 1 (E = 1.875) toward 1/2
+    (E = 1.5), and the reference's online L-BFGS (1e-10 first step, duplicated
+    curvature pairs) stays finite at a small step."""
+    make = {"momentum": lambda: api.MomentumDescent(0.05, 0.5, 1),
+            "nesterov": lambda: api.NesterovMomentum(0.05, 0.5, 1),
+            "lbfgs": lambda: api.OnlineLbfgs(0.02, 2, 1)}[name]
+    wf = api.WaveFunction(ctx, S.sho_gaussian(1.0, 1.0))
+    wk = api.Walkers(wf, 4096, seed=5)
+    p0 = wf.parameters().copy()
+    rec = []
+    vmc = api.VmcRunner(api.Sampler(wf, api.MetropolisDiffuse(0.1), wk), make())
+    _, energies, _, _ = vmc.run_optimization(
+        12, 100, 10, callback=lambda it, r, w: rec.append((r.energy_gradient(), w.parameters().copy())))
+    opt, p = make(), p0
+    for g, p_after in rec:
+        p = p + opt.compute_parameter_update(p, _Grad(g))
+        np.testing.assert_allclose(p, p_after, rtol=1e-12, atol=1e-15)
+    assert np.all(np.isfinite(energies))
+    if name != "lbfgs":
+        assert energies[-1] < energies[0] - 0.05
+
+
 def test_vmc_energy_statistics_fp64_vs_mixed(ctx):
     # helium singlet (alpha 1.6875, beta 0.3): the mixed form agrees with FP64 within 2 sigma
     res = {}
