@@ -515,8 +515,7 @@ def df64_leg(ctx, wf64, make, timed, sr_step, e2e, args, W, sweeps, block, world
     out["roofline"] = {"bound": "fp32 issue (FMA pipe)", "fp64_equivalent_tflops": eq, "fp64_peak_tflops": fp64_peak / 1e3,
                        "fp64_equivalent_frac": eq / (fp64_peak / 1e3),
                        "note": "algorithmic FP64 flops of the formulas (flop_model) over the kernel time: the "
-                               "double-float kernel exceeds the FP64 pipe's peak; its own bound is FP32 issue "
-                               "(profiles/vmc_kernel_h2_df64.md)"}
+                               "double-float kernel exceeds the FP64 pipe's peak; its own bound is FP32 issue"}
     # identical positions, parameters and random streams: native FP64 against double-float
     pos = wk.positions()
     cmp = {}
@@ -545,7 +544,18 @@ def torch_sync():
     torch.cuda.synchronize()
 
 
+def workload_config(walkers: int, sweeps: int, block: int, precision: str, world: int) -> dict:
+    """The config object both arms print for the headline workload."""
+    return {"workload": WORKLOAD, "walkers_per_gpu": walkers, "sweeps_per_step": sweeps, "block_size": block,
+            "sr_params": 2, "precision": precision, "parallelism": f"replicas x{world}",
+            "l2": "GPU arm: L2 flushed between steps (256 MiB write); walker state 3 MiB"}
+
+
 def run_reference(args):
+    """The reference's CPU path (its call pattern restated in oracle/faithful.cpp)
+    on the headline workload itself: every step is one SR iteration's sampling,
+    args.walkers walkers x args.sweeps sweeps with E_L and the SR sums, split over
+    all host threads like VmcRunner's rayon workers."""
     rank, world, _ = dist_info()
     if rank != 0:
         return
@@ -553,7 +563,7 @@ def run_reference(args):
 
     O.build()
     threads = O.hardware_threads()
-    walkers, sweeps = 256 * threads, 1000
+    walkers, sweeps = args.walkers, args.sweeps
     for _ in range(args.warmup):
         cpu_baseline_sample(threads, walkers, 20)
     rates, secs = [], 0.0
@@ -565,10 +575,11 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "walker-steps/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "walkers_per_step_sample": walkers, "sweeps_per_step_sample": sweeps},
+            "config": workload_config(walkers, sweeps, args.block, "fp64", 1),
             "cpu_baseline": {"value": value, "unit": "walker-steps/s", "cores": threads, "kind": "port",
-                             "sample": f"{walkers} walkers x {sweeps} sweeps per step, reference call pattern "
-                                       "(oracle/faithful.cpp), std::thread over all host cores"},
+                             "sample": f"the whole workload: {walkers} walkers x {sweeps} sweeps per step (warm-up "
+                                       "steps 20 sweeps), reference call pattern (oracle/faithful.cpp), std::thread "
+                                       "over all host cores"},
             "e2e": {"value": value, "unit": "walker-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -672,14 +683,12 @@ def main():
     per_launch = work.flops * ws_per_step
     achieved = per_launch / (k_ms / k_n * 1e-3) / 1e12
     peak = (fp64_peak if prec == api.PREC_FP64 else fp32_peak) / 1e3
-    # DRAM bytes per launch from the ncu capture of this kernel (profiles/vmc_kernel_h2_fp64.md,
-    # 65,536 walkers x 50 sweeps: 3.35 MB read, 0 written): the walker state is register-resident,
-    # so a launch reads the positions once whatever its sweep count
-    traffic = 3.35e6 if prec == api.PREC_FP64 else None
+    # the walker state is register-resident: a launch moves only its positions
+    # (in once, out once), whatever its sweep count; the DRAM traffic measured
+    # by ncu is in the kernel's committed profile summary, not in this line
     roofline = {"bound": "fp64" if prec == api.PREC_FP64 else "fp32", "achieved": achieved, "peak": peak,
-                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
-                "traffic_note": "dram__bytes_read + write per launch from an ncu capture of the same kernel at "
-                                "50 sweeps; it does not grow with sweeps (register-resident walkers)",
+                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                "algorithmic_bytes_per_launch": 2 * W * 6 * 8,
                 "kernel": "vmc_kernel<1,1,double,2,false>" if prec == api.PREC_FP64 else "vmc_kernel<1,1,float,2,false>",
                 "kernel_ms_per_launch": k_ms / k_n, "kernel_share_of_step": k_ms / ms,
                 "host_wall_ms_per_step": 1e3 * host_s / args.steps, "step_ms": device_step_ms,
@@ -690,9 +699,7 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": "walker-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if prec == api.PREC_FP64 else "f32/f64-mixed", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "walkers_per_gpu": W, "sweeps_per_step": sweeps, "block_size": block,
-                       "sr_params": 2, "precision": args.precision, "parallelism": f"replicas x{world}",
-                       "l2": "flushed between steps (256 MiB write); walker state 3 MiB"},
+            "config": workload_config(W, sweeps, block, args.precision, world),
             "gpu_launches": args.steps * 3,
             "energy": last.energy, "energy_error": last.error, "acceptance": acc,
             "params": [float(x) for x in wf.parameters()],
