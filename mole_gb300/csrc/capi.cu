@@ -73,6 +73,7 @@ MOLE_DECL_DF(1, 0)
 MOLE_DECL_DF(1, 1)
 MOLE_DECL_DF(2, 1)
 MOLE_DECL_DF(2, 2)
+KernelSetT<double>::Vmc compact_vmc64(int nu, int nd, int slot);
 const NnKernelSetT<double>* nn_kernels_f64_2_2();
 const NnKernelSetT<float>* nn_kernels_f32_2_2();
 
@@ -182,6 +183,21 @@ void fill_params(const mole_system& s, SysParams<R>& sp) {
   sp.vnn_r = (R)vnn;
   sp.nn_theta = s.d_nn_theta;
   sp.nn_tab = s.d_nn_tab;
+  // the FP32 screen's mirror (basis in the kernel's centre order)
+  sp.scr.rmax = 0.f;
+  for (int k = 0; k < 3 * s.n_nuc; ++k) {
+    sp.scr.nuc[k] = (float)s.nuc_pos[k];
+    sp.scr.rmax = std::max(sp.scr.rmax, (float)std::fabs(s.nuc_pos[k]));
+  }
+  for (int j = 0; j < s.n_basis; ++j) {
+    const int b = order[j];
+    sp.scr.zeta[j] = (float)s.theta[s.b_exp[b]];
+    sp.scr.coef[0][j] = s.n_up > 0 ? (float)s.coef_up[b] : 0.f;
+    sp.scr.coef[1][j] = s.n_dn > 0 ? (float)s.coef_dn[b] : 0.f;
+  }
+  sp.scr.cusp_anti = s.ee_on ? (float)s.cusp_anti : 0.f;  // no e-e term: u = 0 in both forms
+  sp.scr.cusp_para = s.ee_on ? (float)s.cusp_para : 0.f;
+  sp.scr.ee_b = s.ee_on ? (float)s.theta[sp.off_ee] : 0.f;
 }
 
 // Re-derives both kernel-parameter images and, for neural systems, the
@@ -230,6 +246,16 @@ KernelSetT<df64>::Vmc vmc_df(const mole_system* s, int slot, int drift) {
   return s->kdf->vmc[slot][0][s->en_on];
 }
 KernelSetT<df64>::Eval eval_df(const mole_system* s) { return s->nn_on || !s->kdf ? nullptr : s->kdf->eval[s->en_on]; }
+// The packed FP64 VMC kernel (compact.cuh) covers FP64 box and Gaussian
+// moves of 1s-STO systems with at most one electron per spin, the plain Pade
+// e-e term (or none), no e-n Jastrow and the Coulomb potential, on ensembles
+// of at least half a wave of its 224-walker CTAs; NULL otherwise.
+KernelSetT<double>::Vmc vmc64_compact(const mole_system* s, int slot, int drift, int W, int n_sm) {
+  if (drift || s->nn_on || s->en_on || s->n_up > 1 || s->n_dn > 1 || s->pot_kind != MOLE_POT_COULOMB) return nullptr;
+  if (s->ee_on && (s->ee_kappa > 0.0 || s->ee_npoly > 0)) return nullptr;
+  if (!s->sp64.all_sto1s || n_sm <= 0 || W < n_sm * kCompactBlock) return nullptr;
+  return compact_vmc64(s->n_up, s->n_dn, slot);
+}
 KernelSetT<double>::Eval eval64(const mole_system* s) { return s->nn_on ? s->nk64->eval : s->k64->eval[s->en_on]; }
 KernelSetT<float>::Eval eval32(const mole_system* s) { return s->nn_on ? s->nk32->eval : s->k32->eval[s->en_on]; }
 KernelSetT<double>::Dmc dmc64(const mole_system* s) { return s->nn_on ? s->nk64->dmc : s->k64->dmc[s->en_on]; }
@@ -752,7 +778,10 @@ int mole_vmc_run(mole_walkers* w, const mole_vmc_opts* o, double* moments, doubl
   auto fdf = o->precision == MOLE_PREC_DF64 ? vmc_df(s, slot, drift) : nullptr;
   if (mixed ? !f32 : !f64) return fail(MOLE_ERR_UNSUPPORTED, "SR kernel not compiled for this family and precision");
   int wpc = kBlock;
-  const int W = w->W, grid = vmc_grid(W, s->n_up, s->n_dn, c->n_sm, &wpc), NA = n_acc(PM);
+  const int W = w->W;
+  auto fcp = (!mixed && !fdf) ? vmc64_compact(s, slot, drift, W, c->n_sm) : nullptr;
+  const int grid = fcp ? compact_grid(W, c->n_sm, &wpc) : vmc_grid(W, s->n_up, s->n_dn, c->n_sm, &wpc);
+  const int NA = n_acc(PM);
   const int n_tb = o->n_steps / o->block_size;
   CUDA_TRY(c->partials.reserve((size_t)grid * NA));
   CUDA_TRY(c->tb_partials.reserve((size_t)grid * std::max(n_tb, 1)));
@@ -781,7 +810,7 @@ int mole_vmc_run(mole_walkers* w, const mole_vmc_opts* o, double* moments, doubl
   Timer tm(c, 0);
   if (mixed) CUDA_TRY(f32(s->sp32, a, grid, c->stream));
   else if (fdf) CUDA_TRY(fdf(s->spdf, a, grid, c->stream));
-  else CUDA_TRY(f64(s->sp64, a, grid, c->stream));
+  else CUDA_TRY((fcp ? fcp : f64)(s->sp64, a, grid, c->stream));
   tm.stop();
   if (fdf) {
     int st = 0;

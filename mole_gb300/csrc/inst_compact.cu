@@ -1,0 +1,19 @@
+// FP64 VMC launchers with the packed FP64 moves (compact.cuh): spin blocks of
+// 1 up and at most 1 down electron, without and with two-parameter SR sums.
+#include "dispatch.cuh"
+
+namespace mole {
+
+template <int NU, int ND, int PM>
+cudaError_t launch_vmc_compact(const SysParams<double>& sp, const VmcArgs& a, int grid, cudaStream_t s) {
+  vmc_compact_kernel<NU, ND, PM><<<grid, kCompactBlock, 0, s>>>(sp, a);
+  return cudaGetLastError();
+}
+
+KernelSetT<double>::Vmc compact_vmc64(int nu, int nd, int slot) {
+  if (nu == 1 && nd == 1) return slot == 0 ? launch_vmc_compact<1, 1, 0> : (slot == 1 ? launch_vmc_compact<1, 1, 2> : nullptr);
+  if (nu == 1 && nd == 0) return slot == 0 ? launch_vmc_compact<1, 0, 0> : (slot == 1 ? launch_vmc_compact<1, 0, 2> : nullptr);
+  return nullptr;
+}
+
+}  // namespace mole

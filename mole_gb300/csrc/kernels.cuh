@@ -1,6 +1,7 @@
 // kernels.cuh -- VMC, evaluation and DMC kernels over a walker ensemble.
 #pragma once
 
+#include "compact.cuh"
 #include "walker.cuh"
 
 namespace mole {
@@ -70,8 +71,12 @@ __device__ __forceinline__ NnCtx<R> nn_setup(const SysParams<R>& sp) {
   return c;
 }
 
-template <int NU, int ND, class R, int PM, bool EN, bool NN, int MOVE>
-__device__ __forceinline__ void vmc_body(const SysParams<R>& sp, const VmcArgs& a, double* red, double* srs) {
+// BLK: threads per CTA; COMPACT: the FP64 moves with packed FP64 work
+// (compact.cuh; R = double, cs its shared-memory slots).
+template <int NU, int ND, class R, int PM, bool EN, bool NN, int MOVE, int BLK = kBlock, bool COMPACT = false,
+          class CS = int>
+__device__ __forceinline__ void vmc_body(const SysParams<R>& sp, const VmcArgs& a, double* red, double* srs,
+                                         CS* cs = nullptr) {
   using Wk = Walker<NU, ND, R, PM, EN, NN>;
   using F = typename Wk::F;  // accumulation type: double, or df64 in the double-float form
   constexpr int NA = n_acc(PM);
@@ -91,13 +96,17 @@ __device__ __forceinline__ void vmc_body(const SysParams<R>& sp, const VmcArgs& 
   double sB2 = 0.0;
   int naccept = 0;
 #pragma unroll
-  for (int k = 0; k < NSR; ++k) srf[k * kBlock + tid] = F(0);
+  for (int k = 0; k < NSR; ++k) srf[k * BLK + tid] = F(0);
   const int total = a.n_eq + a.n_steps;
   const int refresh = a.refresh > 0 ? a.refresh : 100;
   const R step = (R)a.step;
+  const float stepf = (float)a.step;
   for (int it = 0; it < total; ++it) {
     const uint32_t t = a.step0 + (uint32_t)it;
-    naccept += wk.template sweep<MOVE>(sp, step, a.seed, (uint32_t)w, t);
+    if constexpr (COMPACT)
+      naccept += compact_sweep<NU, ND, PM, MOVE>(wk, sp, step, stepf, a.seed, (uint32_t)w, t, active, *cs);
+    else
+      naccept += wk.template sweep<MOVE>(sp, step, a.seed, (uint32_t)w, t);
     if ((it + 1) % refresh == 0) ok = wk.refresh(sp, nullptr, nullptr) && ok;
     if (it < a.n_eq) continue;
     F O[PM > 0 ? PM : 1];
@@ -108,14 +117,14 @@ __device__ __forceinline__ void vmc_body(const SysParams<R>& sp, const VmcArgs& 
     if constexpr (PM > 0) {
 #pragma unroll
       for (int p = 0; p < PM; ++p) {
-        srf[p * kBlock + tid] += O[p];
-        srf[(PM + p) * kBlock + tid] += E * O[p];
+        srf[p * BLK + tid] += O[p];
+        srf[(PM + p) * BLK + tid] += E * O[p];
       }
       int q = 2 * PM;
 #pragma unroll
       for (int p = 0; p < PM; ++p)
 #pragma unroll
-        for (int r = p; r < PM; ++r, ++q) srf[q * kBlock + tid] += O[p] * O[r];
+        for (int r = p; r < PM; ++r, ++q) srf[q * BLK + tid] += O[p] * O[r];
     }
     if ((k + 1) % a.block_size == 0) {
       const double bs = to_d(bsum);
@@ -146,7 +155,7 @@ __device__ __forceinline__ void vmc_body(const SysParams<R>& sp, const VmcArgs& 
   // deterministic CTA reduction, then one partial row per CTA
 #pragma unroll
   for (int k = 0; k < NA; ++k) {
-    double v[1] = {k < kNMom ? acc[k] : (active ? to_d(srf[(k - kNMom) * kBlock + tid]) : 0.0)};
+    double v[1] = {k < kNMom ? acc[k] : (active ? to_d(srf[(k - kNMom) * BLK + tid]) : 0.0)};
     block_sum<1>(v, red);
     if (threadIdx.x == 0) a.partials[(size_t)blockIdx.x * NA + k] = v[0];
   }
@@ -166,6 +175,31 @@ __global__ void __launch_bounds__(kBlock, (min_blocks<NU, ND>())) vmc_kernel(con
     if (a.move == kMoveBox) vmc_body<NU, ND, R, PM, EN, NN, kMoveBox>(sp, a, red, srs);
     else vmc_body<NU, ND, R, PM, EN, NN, kMoveGauss>(sp, a, red, srs);
   }
+}
+
+// FP64 VMC with the packed FP64 moves (compact.cuh): systems with one
+// electron per spin block, box (move 0) and Gaussian moves.
+template <int NU, int ND, int PM>
+// (144 registers: two 224-thread CTAs per SM; launched with kCompactBlock threads)
+__global__ void __maxnreg__(144)
+    vmc_compact_kernel(const __grid_constant__ SysParams<double> sp, const VmcArgs a) {
+  __shared__ double red[kCompactBlock / 32];
+  __shared__ double srs[(n_acc(PM) - kNMom > 0 ? n_acc(PM) - kNMom : 1) * kCompactBlock];
+  __shared__ CompactSlots<NU + ND, PM> cs;
+  if (a.move == kMoveBox)
+    vmc_body<NU, ND, double, PM, false, false, kMoveBox, kCompactBlock, true>(sp, a, red, srs, &cs);
+  else
+    vmc_body<NU, ND, double, PM, false, false, kMoveGauss, kCompactBlock, true>(sp, a, red, srs, &cs);
+}
+
+// Grid of the packed kernel: whole waves of (SMs x 2) CTAs with the walkers
+// split evenly. Sets *wpc (walkers per CTA).
+inline int compact_grid(int W, int n_sm, int* wpc) {
+  const int cap = n_sm * kCompactMinBlocks;
+  const int g = (W + kCompactBlock - 1) / kCompactBlock;
+  const int grid = cap * ((g + cap - 1) / cap);
+  *wpc = (W + grid - 1) / grid;
+  return grid;
 }
 
 struct EvalArgs {

@@ -26,6 +26,16 @@
 
 namespace mole {
 
+// FP32 mirror of what the FP64 kernels' single-precision Metropolis screen
+// reads (compact.cuh): 1s-STO systems with at most one electron per spin.
+struct ScreenParams {
+  float nuc[kMaxNuc * 3];
+  float zeta[kMaxBasis];
+  float coef[2][kMaxBasis];  // orbital 0 of each spin block
+  float rmax;                // largest nuclear coordinate magnitude
+  float cusp_anti, cusp_para, ee_b;
+};
+
 // System description in kernel-parameter memory (broadcast reads).
 template <class R>
 struct SysParams {
@@ -55,6 +65,7 @@ struct SysParams {
   int n_exp, P, off_ee, off_en, off_nn;
   const double* nn_theta;  // device copy of the 9,090 network parameters (neural systems)
   const float* nn_tab;     // quintic tables of the pair networks (neural systems, FP32 form)
+  ScreenParams scr;
 };
 
 template <class R>

@@ -703,7 +703,7 @@ int orc_vmc_run(const orc_system* s, const double* th, int W, double* pos, const
       uint32_t t = o->step0 + (uint32_t)it;
       for (int e = 0; e < N; ++e) {
         mom[ORC_MOM_ACCEPT] += move_electron(s, th, N, p, &cur, e, o->move, o->step, o->seed,
-                                             (uint32_t)w, t);
+                                             o->walker0 + (uint32_t)w, t);
         mom[ORC_MOM_PROPOSED] += 1.0;
       }
       if (it < o->n_eq) continue;

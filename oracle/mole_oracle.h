@@ -115,6 +115,7 @@ typedef struct {
   int32_t sr;          /* accumulate O_k sums */
   uint64_t seed;
   uint32_t step0;      /* global step counter at entry */
+  uint32_t walker0;    /* random-stream index of pos's first walker (a slice of a larger ensemble) */
 } orc_vmc_opts;
 
 /* moments layout (length ORC_NMOM) */

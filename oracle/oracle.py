@@ -63,7 +63,8 @@ class OrcEvalOut(C.Structure):
 
 class OrcVmcOpts(C.Structure):
     _fields_ = [("move", C.c_int32), ("step", C.c_double), ("n_eq", C.c_int32), ("n_steps", C.c_int32),
-                ("block_size", C.c_int32), ("sr", C.c_int32), ("seed", C.c_uint64), ("step0", C.c_uint32)]
+                ("block_size", C.c_int32), ("sr", C.c_int32), ("seed", C.c_uint64), ("step0", C.c_uint32),
+                ("walker0", C.c_uint32)]
 
 
 def _dp(a: np.ndarray):
@@ -169,15 +170,16 @@ def init_positions(W: int, N: int, seed: int, kind: int = 0, width: float = 1.0)
 
 
 def vmc_run(s, pos, *, move: int, step: float, n_eq: int, n_steps: int, block_size: int, sr: bool = False,
-            seed: int = 1, step0: int = 0, theta=None) -> dict:
+            seed: int = 1, step0: int = 0, theta=None, walker0: int = 0) -> dict:
     """Runs the chains in pos (copied, returned updated) with the GPU path's
-    random streams; returns moments, time-block sums and SR sums."""
+    random streams (walker k of pos draws stream walker0 + k); returns
+    moments, time-block sums and SR sums."""
     o = to_orc(s)
     th = np.ascontiguousarray(s.params() if theta is None else theta, dtype=np.float64)
     P = th.size
     pos = np.ascontiguousarray(pos, dtype=np.float64).copy()
     W = pos.shape[0]
-    opts = OrcVmcOpts(move, step, n_eq, n_steps, block_size, int(sr), seed, step0)
+    opts = OrcVmcOpts(move, step, n_eq, n_steps, block_size, int(sr), seed, step0, walker0)
     mom = np.zeros(NMOM)
     tb = np.zeros(max(n_steps // block_size, 1))
     sO, sEO, sOO = np.zeros(max(P, 1)), np.zeros(max(P, 1)), np.zeros(max(P * P, 1))
@@ -187,6 +189,25 @@ def vmc_run(s, pos, *, move: int, step: float, n_eq: int, n_steps: int, block_si
         raise FloatingPointError("oracle VMC failed")
     return {"pos": pos, "moments": mom, "time_blocks": tb[: n_steps // block_size], "sum_O": sO[:P],
             "sum_EO": sEO[:P], "sum_OO": sOO[: P * P].reshape(P, P)}
+
+
+def vmc_run_threads(s, pos, *, threads: int = 0, chunk: int = 4096, **kw) -> dict:
+    """vmc_run over a large ensemble, split into slices of `chunk` walkers run
+    on host threads (ctypes releases the GIL); every slice keeps its walkers'
+    random streams, and the additive sums are added in slice order."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    W = pos.shape[0]
+    starts = list(range(0, W, chunk))
+    threads = threads or hardware_threads()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        parts = list(ex.map(lambda a: vmc_run(s, pos[a:a + chunk], walker0=a, **kw), starts))
+    out = {"pos": np.concatenate([p["pos"] for p in parts])}
+    for k in ("moments", "time_blocks", "sum_O", "sum_EO", "sum_OO"):
+        out[k] = sum(p[k] for p in parts)
+    # counts are per walker in the oracle as in the kernels
+    return out
 
 
 def dmc_step(s, pos, eloc, *, tau: float, e_ref: float, seed: int, step: int, theta=None):
