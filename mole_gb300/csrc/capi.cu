@@ -249,7 +249,7 @@ KernelSetT<df64>::Eval eval_df(const mole_system* s) { return s->nn_on || !s->kd
 // The packed FP64 VMC kernel (compact.cuh) covers FP64 box and Gaussian
 // moves of 1s-STO systems with at most one electron per spin, the plain Pade
 // e-e term (or none), no e-n Jastrow and the Coulomb potential, on ensembles
-// of at least half a wave of its 224-walker CTAs; NULL otherwise.
+// of at least half a wave of its 224-thread CTAs; NULL otherwise.
 KernelSetT<double>::Vmc vmc64_compact(const mole_system* s, int slot, int drift, int W, int n_sm) {
   if (drift || s->nn_on || s->en_on || s->n_up > 1 || s->n_dn > 1 || s->pot_kind != MOLE_POT_COULOMB) return nullptr;
   if (s->ee_on && (s->ee_kappa > 0.0 || s->ee_npoly > 0)) return nullptr;

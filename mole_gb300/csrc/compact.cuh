@@ -29,6 +29,16 @@
 // the FP64 one: the trajectories are those of the one-thread-per-walker
 // kernel, bit for bit.
 //
+// Layout: two 7-warp CTAs per SM (216 walkers each at 65,536 walkers) at most
+// 128 registers, so that the 14 warps fit the four SM sub-partitions'
+// 16,384-register files. Measured on H2 (65,536 walkers, Gaussian 0.4,
+// two-parameter SR sums): FP64-pipe instructions per walker-step 211 -> 181,
+// the launch 53.5 -> 51.5 ms; the gain is bounded because a sub-partition
+// holds only ~3.5 walker warps, so its FP64 work shrinks by whole warps, and
+// the FP64 pipe idles while both CTAs screen (pipe busy 80 % -> 71 %). Four
+// 4-warp CTAs (201 instructions, 55.7 ms) and three 5-warp CTAs (196, 54.4
+// ms) did worse.
+//
 // Scope: the FP64 box and Gaussian moves of systems with at most one electron
 // per spin (He, H2, H, H2+), a basis of 1s STOs, the Pade e-e term without
 // scaled distance or polynomial terms, no e-n Jastrow, Coulomb potential --

@@ -4,8 +4,15 @@
 
 namespace mole {
 
+// Two CTAs (2 x ~44 KB of static shared memory) must fit an SM: the kernel
+// asks for the largest shared-memory carveout, which the default choice does
+// need not give.
 template <int NU, int ND, int PM>
 cudaError_t launch_vmc_compact(const SysParams<double>& sp, const VmcArgs& a, int grid, cudaStream_t s) {
+  static const cudaError_t attr = cudaFuncSetAttribute(vmc_compact_kernel<NU, ND, PM>,
+                                                       cudaFuncAttributePreferredSharedMemoryCarveout,
+                                                       (int)cudaSharedmemCarveoutMaxShared);
+  if (attr != cudaSuccess) return attr;
   vmc_compact_kernel<NU, ND, PM><<<grid, kCompactBlock, 0, s>>>(sp, a);
   return cudaGetLastError();
 }

@@ -180,8 +180,9 @@ __global__ void __launch_bounds__(kBlock, (min_blocks<NU, ND>())) vmc_kernel(con
 // FP64 VMC with the packed FP64 moves (compact.cuh): systems with one
 // electron per spin block, box (move 0) and Gaussian moves.
 template <int NU, int ND, int PM>
-// (144 registers: two 224-thread CTAs per SM; launched with kCompactBlock threads)
-__global__ void __maxnreg__(144)
+// (128 registers: two 7-warp CTAs per SM -- four of their 14 warps share an
+// SM sub-partition and its 16,384 registers; launched with kCompactBlock threads)
+__global__ void __maxnreg__(128)
     vmc_compact_kernel(const __grid_constant__ SysParams<double> sp, const VmcArgs a) {
   __shared__ double red[kCompactBlock / 32];
   __shared__ double srs[(n_acc(PM) - kNMom > 0 ? n_acc(PM) - kNMom : 1) * kCompactBlock];

@@ -3,7 +3,7 @@
 The other parity tests run tens to hundreds of walkers; these run the
 workloads' own ensembles through the same C ABI calls, so the launch shapes
 the bench times -- whole waves of SMs x resident CTAs with the walkers split
-evenly, the packed FP64 kernel (224-walker CTAs, FP32-screened proposals
+evenly, the packed FP64 kernel (224-thread CTAs, FP32-screened proposals
 whose FP64 evaluation is packed across warps), ~1,000 CTAs of partial sums
 reduced in a fixed order, the ragged batch's persistent work queue, the
 multi-block comb scan -- are checked against the CPU oracle on the same
@@ -15,7 +15,8 @@ random streams:
   walkers in native FP64 (packed kernel) and in the double-float form;
 * a hydrogen atom (1s STO) at 40,000 walkers with SR sums (the packed
   kernel's one-electron form);
-* Be DMC (Pade guide), 131,072 walkers, tau 0.005, comb every step;
+* Be DMC (Pade guide), 131,072 VMC-equilibrated walkers, tau 0.005, comb
+  every step;
 * the full 256-system ragged batch (583,055 walkers, N = 2..10) in FP64.
 
 The bar is the trajectory bar of the smaller tests: positions to 1e-9,
@@ -78,17 +79,24 @@ def test_vmc_at_workload_size_matches_oracle(ctx, name, W, move, step, prec, sr)
 
 
 def test_be_dmc_at_workload_size_matches_oracle(ctx):
+    """From VMC-equilibrated walkers, as the DMC workload starts. (An
+    unequilibrated N(0, 1) ensemble of this size holds walkers within ~1e-6
+    bohr of a node, where the reference's drift-diffusion rule throws an
+    electron hundreds of bohr and rounding at 1e-16 decides the outcome; one
+    such walker's weight then takes over the comb.)"""
     s = S.beryllium()
     wf = api.WaveFunction(ctx, s)
     W, tau = 131072, 0.005
     wk = api.Walkers(wf, W, seed=0x5EED + 5)
+    api.Sampler(wf, api.MetropolisGaussian(0.3), wk).run(200, 0, 1)
     pos = wk.positions()
+    t0 = wk.step  # the DMC steps continue the walkers' random-stream position
     el = O.evaluate(s, pos, want_O=False)["eloc"]
     dmc = api.DmcRunner(wf, wk, reference_energy=-14.6)
     e_gpu = dmc.run_block(tau, 2)
     e_ref, acc = [], 0.0
     for t in range(2):
-        r = O.dmc_step(s, pos, el, tau=tau, e_ref=-14.6, seed=0x5EED + 5, step=t)
+        r = O.dmc_step(s, pos, el, tau=tau, e_ref=-14.6, seed=0x5EED + 5, step=t0 + t)
         pos, el = r["pos"], r["eloc"]
         e_ref.append(r["energy"])
         acc += r["accepted"]
