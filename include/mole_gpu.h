@@ -244,10 +244,14 @@ int mole_vmc_run(mole_walkers* w, const mole_vmc_opts* opts, double* moments, do
  * library holds until the process exits; the call is rejected with
  * MOLE_ERR_SHAPE when (CTAs of the launch) x (accumulators + time blocks) does not
  * fit it. The first call on a device looks up that array's device address,
- * so make it before any stream capture. Every call shares the array: calls
- * that overlap on the GPU (other streams, other threads) race. The call
- * synchronises `stream` (a cudaStream_t, NULL for the default stream) before
- * returning. */
+ * so make it before any stream capture; the address is kept for the life of
+ * the process and stays valid while the device's primary context lives (a
+ * cudaDeviceReset by the caller invalidates it). Every call shares the array:
+ * calls that overlap on the GPU (other streams, other threads) race. The call
+ * reads its status word back and synchronises `stream` (a cudaStream_t of the
+ * system's device, NULL for the default stream; a stream of another device is
+ * rejected with MOLE_ERR_INVALID_ARG) before returning, and leaves the
+ * caller's current device as it found it. */
 int mole_vmc_run_noalloc(const mole_system* sys, double* d_pos, int32_t n_walkers, uint64_t seed, uint64_t step0,
                          const mole_vmc_opts* opts, double* d_moments, double* d_time_blocks, double* d_sr,
                          void* stream);

@@ -866,7 +866,20 @@ namespace {
 std::mutex g_noalloc_mu;
 double* g_noalloc_addr[256] = {nullptr};
 
-// Device address of the scratch array on `device` (which must be current).
+// Restores the caller's current device when the entry point returns.
+struct DeviceRestore {
+  int prev = -1;
+  DeviceRestore() {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+  }
+  ~DeviceRestore() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+// Device address of the scratch array on `device` (which must be current),
+// looked up once per device: it stays valid while the device's primary
+// context lives (for the whole process unless the caller resets the device).
 cudaError_t noalloc_scratch(int device, double** out) {
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
   if (device < 0 || device >= 256) return cudaErrorInvalidDevice;
@@ -917,11 +930,17 @@ int mole_vmc_run_noalloc(const mole_system* s, double* d_pos, int32_t W, uint64_
                                     " bytes of scratch; the allocation-free entry point has " +
                                     std::to_string(kNoAllocScratchDoubles * 8));
   if (n_tb > 0 && !d_time_blocks) return fail(MOLE_ERR_DATA_ACCESS, "time_blocks output is NULL");
+  DeviceRestore restore;  // the caller's current device is left as it was
   CUDA_TRY(cudaSetDevice(s->ctx->device));
   cudaGetLastError();  // report only errors raised by this call
+  cudaStream_t st = (cudaStream_t)stream;
+  int st_dev = -1;
+  CUDA_TRY(cudaStreamGetDevice(st, &st_dev));
+  if (st_dev != s->ctx->device)
+    return fail(MOLE_ERR_INVALID_ARG, "the stream belongs to device " + std::to_string(st_dev) +
+                                          ", the system to device " + std::to_string(s->ctx->device));
   double* scratch = nullptr;
   CUDA_TRY(noalloc_scratch(s->ctx->device, &scratch));
-  cudaStream_t st = (cudaStream_t)stream;
   double* partials = scratch;
   double* tb_partials = partials + (size_t)grid * NA;
   double* reduced = tb_partials + (size_t)grid * n_tb;
