@@ -689,7 +689,8 @@ def main():
     roofline = {"bound": "fp64" if prec == api.PREC_FP64 else "fp32", "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
                 "algorithmic_bytes_per_launch": 2 * W * 6 * 8,
-                "kernel": "vmc_kernel<1,1,double,2,false>" if prec == api.PREC_FP64 else "vmc_kernel<1,1,float,2,false>",
+                "kernel": "vmc_compact_kernel<1,1,2> (FP64 moves packed across warps)" if prec == api.PREC_FP64
+                else "vmc_kernel<1,1,float,2,false>",
                 "kernel_ms_per_launch": k_ms / k_n, "kernel_share_of_step": k_ms / ms,
                 "host_wall_ms_per_step": 1e3 * host_s / args.steps, "step_ms": device_step_ms,
                 "flops_per_walker_step": work.flops,
