@@ -45,13 +45,65 @@ def parse():
     p.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "df64"])
     p.add_argument("--no-extras", action="store_true", help="skip the e2e, mixed and CPU-baseline legs")
     p.add_argument("--no-clocks", action="store_true", help="do not sample nvidia-smi during the timed region")
-    p.add_argument("--case", default=None, choices=["h2-vmc", "lih-nn-vmc", "sgemm", "be-dmc", "ragged-batch"],
+    p.add_argument("--case", default=None, choices=["h2-vmc", "lih-nn-vmc", "sgemm", "be-dmc", "ragged-batch",
+                                                     "long-c4", "long-c5"],
                    help="run one small kernel case (for profiling) and exit")
     return p.parse_args()
 
 
+def long_c4(ctx, iters: int = 500, steps: int = 1000, W: int = 16384) -> dict:
+    """LiH at its workload's full length: 16,384 walkers, SR iterations of
+    `steps` sweeps (500 x 1,000), from the same start, for the Pade-Jastrow
+    fallback in FP64 (SR over the 4 orbital/Pade parameters) and the pair-
+    network Jastrow in the mixed form (SR over all 9,094 parameters, S on the
+    tensor cores). Each trained wave function is then sampled for 4,000
+    sweeps; the trained network also in the FP64 form (the network evaluated
+    directly in FP64) on the same walkers: its energy difference is the mixed
+    form's error."""
+    import numpy as np
+    import torch
+
+    from mole_gb300 import api
+    from mole_gb300 import system as S
+
+    out = {"workload": f"LiH VMC + SR, {W} walkers, {iters} SR iterations x {steps} sweeps", "walkers": W}
+
+    def final(samp, sweeps=4000):
+        samp.run(100, 0, 1)
+        r = samp.run(0, sweeps, 100)
+        return {"energy": r.energy, "error": r.error, "variance": r.variance, "acceptance": r.acceptance}
+
+    for name, neural, prec in (("pade_fp64", False, api.PREC_FP64), ("neural_mixed", True, api.PREC_MIXED)):
+        s = S.lih(neural=neural, rng=np.random.default_rng(1))
+        wf = api.WaveFunction(ctx, s)
+        wk = api.Walkers(wf, W, seed=0x5EED + 4)
+        samp = api.Sampler(wf, api.MetropolisGaussian(0.3), wk, precision=prec)
+        samp.run(300, 0, 1)
+        sr = api.StochasticReconfiguration(0.05, 1e-3, samples=4, sample_every=10, precision=prec)
+        t0 = time.perf_counter()
+        _, en, er, _ = api.VmcRunner(samp, sr).run_optimization(iters, steps, 100)
+        torch.cuda.synchronize()
+        leg = {"train_s": time.perf_counter() - t0, "train_energy_first": float(en[0]),
+               "train_energy_last": float(en[-1]), "train_curve_every_50": [float(x) for x in en[::50]]}
+        leg.update(final(samp))
+        if neural:
+            s64 = api.Sampler(wf, api.MetropolisGaussian(0.3), wk, precision=api.PREC_FP64)
+            f64 = final(s64, 1000)
+            leg["fp64_same_network"] = f64
+            leg["energy_delta_vs_fp64"] = leg["energy"] - f64["energy"]
+            leg["delta_sigma"] = float(np.hypot(leg["error"], f64["error"]))
+        out[name] = leg
+        wk.close()
+        wf.close()
+    out["neural_gain_ha"] = out["pade_fp64"]["energy"] - out["neural_mixed"]["energy"]
+    out["variance_ratio_neural_over_pade"] = out["neural_mixed"]["variance"] / out["pade_fp64"]["variance"]
+    return out
+
+
 def run_case(case: str, precision: str = "fp64") -> None:
-    """Small single-purpose runs whose kernels the committed ncu summaries profile."""
+    """Small single-purpose runs whose kernels the committed ncu summaries
+    profile, and the long runs of the LiH and Be workloads (long-c4,
+    long-c5), which stay outside the default bench."""
     import numpy as np
     import torch
 
@@ -60,6 +112,13 @@ def run_case(case: str, precision: str = "fp64") -> None:
 
     ctx = api.Context(0)
     t0 = time.perf_counter()
+    if case == "long-c4":
+        print(json.dumps({"case": case, **long_c4(ctx), "seconds": time.perf_counter() - t0}, default=_json_default))
+        return
+    if case == "long-c5":
+        r = dmc_leg(ctx, n_eq=2000, n_steps=20000, train_iters=40, raw_eloc_leg=True)
+        print(json.dumps({"case": case, **r, "seconds": time.perf_counter() - t0}, default=_json_default))
+        return
     if case == "h2-vmc":
         prec = {"fp64": api.PREC_FP64, "mixed": api.PREC_MIXED, "df64": api.PREC_DF64}[precision]
         wf = api.WaveFunction(ctx, S.h2(1.0, 0.5))
@@ -403,7 +462,7 @@ def helium_leg(ctx) -> dict:
     return out
 
 
-def dmc_leg(ctx, n_eq: int = 2000, n_steps: int = 800, train_iters: int = 20) -> dict:
+def dmc_leg(ctx, n_eq: int = 2000, n_steps: int = 800, train_iters: int = 20, raw_eloc_leg: bool = False) -> dict:
     """DMC on the Be atom (Z = 4, 2 up + 2 down, 1s/2s STO determinant):
     131,072 walkers, time step 0.005, drift-diffusion moves with Metropolis
     accept/reject, a stochastic comb every step, FP64 weights and energy
@@ -426,14 +485,14 @@ def dmc_leg(ctx, n_eq: int = 2000, n_steps: int = 800, train_iters: int = 20) ->
 
     cut = 2.0 / np.sqrt(tau)  # E_L window of the weight factor (Umrigar-Nightingale-Runge)
 
-    def run(system, prec, steps, label):
+    def run(system, prec, steps, label, cutoff=cut):
         wf = api.WaveFunction(ctx, system)
         wk = api.Walkers(wf, W, seed=0x5EED + 5)
         # VMC equilibration with Gaussian moves: the reference's drift-diffusion
         # acceptance accepts any proposal next to a node (see DmcRunner)
         api.Sampler(wf, api.MetropolisGaussian(0.3), wk, precision=prec).run(200, 0, 1)
         e_ref = api.Sampler(wf, api.MetropolisGaussian(0.3), wk, precision=prec).run(0, 20, 10).energy
-        dmc = api.DmcRunner(wf, wk, e_ref, precision=prec, eloc_cutoff=cut)
+        dmc = api.DmcRunner(wf, wk, e_ref, precision=prec, eloc_cutoff=cutoff)
         e_eq = dmc.run_block(tau, n_eq)
         dmc.reference_energy = float(np.mean(e_eq[-50:]))
         ctx.enable_timing(True)
@@ -463,6 +522,10 @@ def dmc_leg(ctx, n_eq: int = 2000, n_steps: int = 800, train_iters: int = 20) ->
     out["pade_df64"] = run(pade, api.PREC_DF64, n_steps, "pade_df64")
     out["pade_df64"]["fp64_reruns"] = ctx.df64_reruns() - r0
     out["pade_df64"]["energy_delta_vs_fp64"] = out["pade_df64"]["energy"] - f["energy"]
+    if raw_eloc_leg:
+        # the reference's weights: the raw E_L, no window (dmc.rs:126-128)
+        out["pade_fp64_raw_eloc"] = run(pade, api.PREC_FP64, n_steps, "pade64_raw", cutoff=0.0)
+        out["pade_fp64_raw_eloc"]["energy_delta_vs_clipped"] = out["pade_fp64_raw_eloc"]["energy"] - f["energy"]
     # neural guide: pair networks trained on Be by VMC + SR from Gaussian(0, 0.01^2) weights
     s = S.beryllium(neural=True, rng=np.random.default_rng(5))
     wf = api.WaveFunction(ctx, s)

@@ -17,7 +17,10 @@ random streams:
   kernel's one-electron form);
 * Be DMC (Pade guide), 131,072 VMC-equilibrated walkers, tau 0.005, comb
   every step;
-* the full 256-system ragged batch (583,055 walkers, N = 2..10) in FP64.
+* the full 256-system ragged batch (583,055 walkers, N = 2..10) in FP64;
+* LiH with the pair networks at 16,384 walkers: evaluation against the oracle,
+  and one full SR sample's tensor-core S matrix within the bound its BF16
+  operands and FP32 tile sums allow.
 
 The bar is the trajectory bar of the smaller tests: positions to 1e-9,
 identical acceptance counts, sums to 1e-9.
@@ -128,3 +131,67 @@ def test_full_ragged_batch_matches_oracle(ctx):
         assert m[O.MOM_ACCEPT] == rm[O.MOM_ACCEPT] and m[O.MOM_PROPOSED] == rm[O.MOM_PROPOSED], systems[k].name
         for j in (O.MOM_SUM_E, O.MOM_SUM_E2, O.MOM_SUM_BLOCK2):
             assert close(m[j], rm[j]) < 1e-9, (systems[k].name, j)
+
+
+def lih_nn(std=0.1, seed=5):
+    s = S.lih(neural=True, rng=np.random.default_rng(seed))
+    w = np.random.default_rng(seed).normal(0.0, std, size=S.NN_P)
+    return s.with_params(np.concatenate([s.params()[:-S.NN_P], w]))
+
+
+def test_lih_neural_evaluation_at_workload_size(ctx):
+    """LiH with the pair networks, 16,384 walkers (its workload's ensemble):
+    ln psi, sign, grad ln psi, lap psi / psi and E_L of the FP64 form against
+    the oracle at 1e-10, and the network O_k of the first 1,024 walkers within
+    the network bar of the smaller test (FP32 backward pass, 2e-4)."""
+    s = lih_nn(std=0.2)
+    wf = api.WaveFunction(ctx, s)
+    W = 16384
+    wk = api.Walkers(wf, W, seed=0x5EED + 4)
+    api.Sampler(wf, api.MetropolisGaussian(0.3), wk, precision=api.PREC_MIXED).run(50, 0, 1)
+    pos = wk.positions()
+    g = wk.evaluate(api.PREC_FP64, want_O=False)
+    r = O.evaluate(s, pos, want_O=False)
+    for k in ("lnpsi", "grad", "lap", "eloc"):
+        assert close(g[k], r[k]) < 1e-10, k
+    assert np.all(g["sign"] == r["sign"])
+    sub = api.Walkers(wf, 1024, seed=1)
+    sub.set_positions(pos[:1024])
+    go = sub.evaluate(api.PREC_FP64)["O"]
+    ro = O.evaluate(s, pos[:1024])["O"]
+    nw = s.n_params - S.NN_P
+    np.testing.assert_allclose(go[:, :nw], ro[:, :nw], rtol=1e-10, atol=1e-10)
+    assert np.max(np.abs(go[:, nw:] - ro[:, nw:]) / np.maximum(1.0, np.abs(ro[:, nw:]))) < 2e-4
+
+
+def test_s_matrix_of_one_full_sample_within_bf16_bound(ctx):
+    """One SR sample of the LiH neural workload (16,384 walkers, 9,094
+    parameters): the tcgen05 S matrix against float64 numpy on the O_k the
+    evaluation returns. The GEMM's operands are a = bf16(O - c) (unit roundoff
+    2^-8, so a product carries at most 2^-7 relative error) summed in FP32
+    inside a tile over the sample's K = 16,384 walkers (at most K 2^-24 of the
+    sum of magnitudes), so |S_gpu - S_ref|_ij <= (2^-7 + K 2^-24) B_ij with
+    B_ij = sum_k |a_ki| |a_kj| / K; checked on 320 rows (the orbital/Pade
+    parameters, both networks' first and last layers) against every column."""
+    s = lih_nn(std=0.1)
+    wf = api.WaveFunction(ctx, s)
+    W = 16384
+    wk = api.Walkers(wf, W, seed=9)
+    api.Sampler(wf, api.MetropolisGaussian(0.3), wk, precision=api.PREC_MIXED).run(50, 0, 1)
+    ev = wk.evaluate(api.PREC_MIXED)
+    wk.sr_collect_begin()
+    wk.sr_collect_sample(api.PREC_MIXED)
+    eps = 1e-3
+    S_gpu = wk.sr_collect_matrix(eps)
+    Ob = ev["O"]
+    A = Ob - Ob.mean(axis=0)
+    P = Ob.shape[1]
+    rng = np.random.default_rng(0)
+    rows = np.unique(np.concatenate([np.arange(8), np.arange(P - 64, P), rng.choice(P, 248, replace=False)]))
+    S_ref = A[:, rows].T @ A / W
+    S_ref[np.arange(rows.size), rows] += eps
+    B = np.abs(A[:, rows]).T @ np.abs(A) / W
+    bound = (2.0 ** -7 + W * 2.0 ** -24) * B + 1e-12
+    err = np.abs(S_gpu[rows] - S_ref)
+    assert np.all(err <= bound), float(np.max(err / bound))
+    assert np.allclose(S_gpu, S_gpu.T)
