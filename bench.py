@@ -79,7 +79,7 @@ def long_c4(ctx, iters: int = 500, steps: int = 1000, W: int = 16384) -> dict:
         wk = api.Walkers(wf, W, seed=0x5EED + 4)
         samp = api.Sampler(wf, api.MetropolisGaussian(0.3), wk, precision=prec)
         samp.run(300, 0, 1)
-        sr = api.StochasticReconfiguration(0.05, 1e-3, samples=4, sample_every=10, precision=prec)
+        sr = api.StochasticReconfiguration(0.05, 1e-3, samples=4, sample_every=10, precision=prec, max_iter=2000)
         t0 = time.perf_counter()
         _, en, er, _ = api.VmcRunner(samp, sr).run_optimization(iters, steps, 100)
         torch.cuda.synchronize()

@@ -494,9 +494,10 @@ class StochasticReconfiguration:
     tensor cores and solved by conjugate gradients."""
 
     def __init__(self, step_size: float, eps: float = 1e-3, samples: int = 8, sample_every: int = 10,
-                 precision: int = PREC_MIXED):
+                 precision: int = PREC_MIXED, max_iter: int = 500):
         self.step_size, self.eps = step_size, eps
         self.samples, self.sample_every, self.precision = samples, sample_every, precision
+        self.max_iter = max_iter
         self.last_info = None
 
     def collect_and_solve(self, sampler: "Sampler"):
@@ -505,7 +506,14 @@ class StochasticReconfiguration:
         for _ in range(self.samples):
             sampler.run(0, self.sample_every, self.sample_every)
             wk.sr_collect_sample(self.precision)
-        delta, g, info = wk.sr_collect_solve(self.eps, self.step_size)
+        try:
+            delta, g, info = wk.sr_collect_solve(self.eps, self.step_size, max_iter=self.max_iter)
+        except MoleError as e:
+            # an ill-conditioned S (late in a long training) can need more CG
+            # iterations: one retry with four times as many, then the error
+            if e.kind != "LinalgError":
+                raise
+            delta, g, info = wk.sr_collect_solve(self.eps, self.step_size, max_iter=4 * self.max_iter)
         self.last_info = info
         return delta, g
 
