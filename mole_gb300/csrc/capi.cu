@@ -74,6 +74,7 @@ MOLE_DECL_DF(1, 1)
 MOLE_DECL_DF(2, 1)
 MOLE_DECL_DF(2, 2)
 KernelSetT<double>::Vmc compact_vmc64(int nu, int nd, int slot);
+KernelSetT<double>::Vmc team_vmc64(int nu, int nd, int slot);
 const NnKernelSetT<double>* nn_kernels_f64_2_2();
 const NnKernelSetT<float>* nn_kernels_f32_2_2();
 
@@ -250,11 +251,20 @@ KernelSetT<df64>::Eval eval_df(const mole_system* s) { return s->nn_on || !s->kd
 // moves of 1s-STO systems with at most one electron per spin, the plain Pade
 // e-e term (or none), no e-n Jastrow and the Coulomb potential, on ensembles
 // of at least half a wave of its 224-thread CTAs; NULL otherwise.
+bool one_electron_per_spin_1s(const mole_system* s, int drift) {
+  if (drift || s->nn_on || s->en_on || s->n_up > 1 || s->n_dn > 1 || s->pot_kind != MOLE_POT_COULOMB) return false;
+  if (s->ee_on && (s->ee_kappa > 0.0 || s->ee_npoly > 0)) return false;
+  return s->sp64.all_sto1s;
+}
 KernelSetT<double>::Vmc vmc64_compact(const mole_system* s, int slot, int drift, int W, int n_sm) {
-  if (drift || s->nn_on || s->en_on || s->n_up > 1 || s->n_dn > 1 || s->pot_kind != MOLE_POT_COULOMB) return nullptr;
-  if (s->ee_on && (s->ee_kappa > 0.0 || s->ee_npoly > 0)) return nullptr;
-  if (!s->sp64.all_sto1s || n_sm <= 0 || W < n_sm * kCompactBlock) return nullptr;
+  if (!one_electron_per_spin_1s(s, drift) || n_sm <= 0 || W < n_sm * kCompactBlock) return nullptr;
   return compact_vmc64(s->n_up, s->n_dn, slot);
+}
+// The same systems on small ensembles (up to two 32-walker teams per SM):
+// the three-warp teams of team.cuh.
+KernelSetT<double>::Vmc vmc64_team(const mole_system* s, int slot, int drift, int W, int n_sm) {
+  if (!one_electron_per_spin_1s(s, drift) || n_sm <= 0 || W > 2 * 32 * n_sm) return nullptr;
+  return team_vmc64(s->n_up, s->n_dn, slot);
 }
 KernelSetT<double>::Eval eval64(const mole_system* s) { return s->nn_on ? s->nk64->eval : s->k64->eval[s->en_on]; }
 KernelSetT<float>::Eval eval32(const mole_system* s) { return s->nn_on ? s->nk32->eval : s->k32->eval[s->en_on]; }
@@ -780,7 +790,10 @@ int mole_vmc_run(mole_walkers* w, const mole_vmc_opts* o, double* moments, doubl
   int wpc = kBlock;
   const int W = w->W;
   auto fcp = (!mixed && !fdf) ? vmc64_compact(s, slot, drift, W, c->n_sm) : nullptr;
-  const int grid = fcp ? compact_grid(W, c->n_sm, &wpc) : vmc_grid(W, s->n_up, s->n_dn, c->n_sm, &wpc);
+  auto ftm = (!mixed && !fdf && !fcp) ? vmc64_team(s, slot, drift, W, c->n_sm) : nullptr;
+  if (ftm) wpc = 32;
+  const int grid = fcp ? compact_grid(W, c->n_sm, &wpc)
+                       : (ftm ? (W + 31) / 32 : vmc_grid(W, s->n_up, s->n_dn, c->n_sm, &wpc));
   const int NA = n_acc(PM);
   const int n_tb = o->n_steps / o->block_size;
   CUDA_TRY(c->partials.reserve((size_t)grid * NA));
@@ -810,7 +823,7 @@ int mole_vmc_run(mole_walkers* w, const mole_vmc_opts* o, double* moments, doubl
   Timer tm(c, 0);
   if (mixed) CUDA_TRY(f32(s->sp32, a, grid, c->stream));
   else if (fdf) CUDA_TRY(fdf(s->spdf, a, grid, c->stream));
-  else CUDA_TRY((fcp ? fcp : f64)(s->sp64, a, grid, c->stream));
+  else CUDA_TRY((fcp ? fcp : (ftm ? ftm : f64))(s->sp64, a, grid, c->stream));
   tm.stop();
   if (fdf) {
     int st = 0;

@@ -1,5 +1,6 @@
-// FP64 VMC launchers with the packed FP64 moves (compact.cuh): spin blocks of
-// 1 up and at most 1 down electron, without and with two-parameter SR sums.
+// FP64 VMC launchers for spin blocks of 1 up and at most 1 down electron,
+// without and with two-parameter SR sums: the packed FP64 moves (compact.cuh,
+// large ensembles) and the three-warp teams (team.cuh, small ensembles).
 #include "dispatch.cuh"
 
 namespace mole {
@@ -15,6 +16,18 @@ cudaError_t launch_vmc_compact(const SysParams<double>& sp, const VmcArgs& a, in
   if (attr != cudaSuccess) return attr;
   vmc_compact_kernel<NU, ND, PM><<<grid, kCompactBlock, 0, s>>>(sp, a);
   return cudaGetLastError();
+}
+
+template <int NU, int ND, int PM>
+cudaError_t launch_vmc_team(const SysParams<double>& sp, const VmcArgs& a, int grid, cudaStream_t s) {
+  vmc_team_kernel<NU, ND, PM><<<grid, kTeamThreads, 0, s>>>(sp, a);
+  return cudaGetLastError();
+}
+
+KernelSetT<double>::Vmc team_vmc64(int nu, int nd, int slot) {
+  if (nu == 1 && nd == 1) return slot == 0 ? launch_vmc_team<1, 1, 0> : (slot == 1 ? launch_vmc_team<1, 1, 2> : nullptr);
+  if (nu == 1 && nd == 0) return slot == 0 ? launch_vmc_team<1, 0, 0> : (slot == 1 ? launch_vmc_team<1, 0, 2> : nullptr);
+  return nullptr;
 }
 
 KernelSetT<double>::Vmc compact_vmc64(int nu, int nd, int slot) {

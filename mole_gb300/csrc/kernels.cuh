@@ -193,6 +193,10 @@ __global__ void __maxnreg__(128)
     vmc_body<NU, ND, double, PM, false, false, kMoveGauss, kCompactBlock, true>(sp, a, red, srs, &cs);
 }
 
+}  // namespace mole
+#include "team.cuh"
+namespace mole {
+
 // Grid of the packed kernel: whole waves of (SMs x 2) CTAs with the walkers
 // split evenly. Sets *wpc (walkers per CTA).
 inline int compact_grid(int W, int n_sm, int* wpc) {
