@@ -112,6 +112,7 @@ def run_case(case: str, precision: str = "fp64") -> None:
 
     ctx = api.Context(0)
     t0 = time.perf_counter()
+    extra = {}
     if case == "long-c4":
         print(json.dumps({"case": case, **long_c4(ctx), "seconds": time.perf_counter() - t0}, default=_json_default))
         return
@@ -134,10 +135,18 @@ def run_case(case: str, precision: str = "fp64") -> None:
         if case == "lih-nn-vmc":
             r = samp.run(0, 20, 10)
         else:
-            wk.sr_collect_begin()
-            for _ in range(2):
-                wk.sr_collect_sample(api.PREC_MIXED)
-            wk.sr_collect_solve(1e-3, 0.05)
+            # two SR iterations of four samples each (one S-GEMM launch per
+            # iteration, K = 65,536); the second is timed
+            for it in range(2):
+                ctx.enable_timing(it == 1)
+                wk.sr_collect_begin()
+                for _ in range(4):
+                    wk.sr_collect_sample(api.PREC_MIXED)
+                wk.sr_collect_solve(1e-3, 0.05)
+            s_ms, s_n = ctx.kernel_time(2)
+            g_ms, g_n = ctx.kernel_time(3)
+            ctx.enable_timing(False)
+            extra = {"sample_ms": s_ms / max(s_n, 1), "s_gemm_ms_per_launch": g_ms / max(g_n, 1)}
             r = None
     elif case == "ragged-batch":
         systems, walkers, widths = api.ragged_batch(64, w_range=(256, 1024))
@@ -153,7 +162,8 @@ def run_case(case: str, precision: str = "fp64") -> None:
         r = dmc.run_block(0.005, 20)
     torch.cuda.synchronize()
     print(json.dumps({"case": case, "seconds": time.perf_counter() - t0,
-                      "energy": None if r is None else float(np.mean(r.energy if hasattr(r, "energy") else r))}))
+                      "energy": None if r is None else float(np.mean(r.energy if hasattr(r, "energy") else r)),
+                      **extra}))
 
 
 def _json_default(o):
@@ -298,7 +308,9 @@ def lih_time_to_sigma(ctx, W: int, train_iters: int, target: float = 1e-3) -> di
                                                         "MLP directly, the mixed form interpolates its tables"})
         if neural and g_n:
             P_pad = (s.n_params + 127) // 128 * 128
-            flops = 2.0 * P_pad * P_pad * ((W + 63) // 64 * 64) * 0.5 * (1 + 128.0 / P_pad)  # upper tiles only
+            # the iteration's 4 samples go through one launch: K = 4 W rows
+            K = (sr.samples * W + 63) // 64 * 64
+            flops = 2.0 * P_pad * P_pad * K * 0.5 * (1 + 128.0 / P_pad)  # upper tiles only
             leg["s_gemm"] = {"ms_per_launch": g_ms / g_n, "tflops": flops / (g_ms / g_n * 1e-3) / 1e12,
                              "peak_bf16_tflops": 1935.3, "peak_source": "MEASURED_PEAKS.json bf16 burst"}
         out[name] = leg

@@ -313,6 +313,7 @@ int mole_ctx_create(int32_t device, mole_ctx** out) {
   mole_ctx* c = new mole_ctx();
   c->device = device;
   cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, device);
+  cudaDeviceGetAttribute(&c->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
   cudaError_t e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
@@ -620,8 +621,8 @@ static void free_dmc(mole_walkers* w) {
   w->eloc_valid = false;
   if (w->srl) {
     SrLargeState* t = w->srl;
-    for (void* p : {(void*)t->O, (void*)t->Ot, (void*)t->S, (void*)t->E, (void*)t->center, (void*)t->sumO,
-                    (void*)t->sumEO, (void*)t->work, (void*)t->status})
+    for (void* p : {(void*)t->O, (void*)t->center, (void*)t->Ob, (void*)t->partial, (void*)t->S, (void*)t->E,
+                    (void*)t->x, (void*)t->sumO, (void*)t->sumEO, (void*)t->work, (void*)t->status})
       if (p) cudaFree(p);
     delete t;
     w->srl = nullptr;
@@ -999,31 +1000,64 @@ int mole_sr_collect_begin(mole_walkers* w) {
     std::memset(t, 0, sizeof(*t));
     t->P = P;
     t->P_pad = (P + kSBM - 1) / kSBM * kSBM;
-    t->K_pad = (W + kSBK - 1) / kSBK * kSBK;
+    const size_t sample_bytes = sizeof(__nv_bfloat16) * (size_t)W * t->P_pad;
+    const int n_samples = (int)std::max<size_t>(1, std::min<size_t>(kObSamples, kObBudget / sample_bytes));
+    t->K_cap = (n_samples * W + kSBK - 1) / kSBK * kSBK;
+    t->n_cta = sr_sample_ctas(W, c->n_sm);
     w->srl = t;  // freed by free_dmc on failure below
-    CUDA_TRY(cudaMalloc(&t->O, sizeof(float) * (size_t)W * P));
-    CUDA_TRY(cudaMalloc(&t->Ot, sizeof(__nv_bfloat16) * (size_t)t->P_pad * t->K_pad));
-    CUDA_TRY(cudaMemset(t->Ot, 0, sizeof(__nv_bfloat16) * (size_t)t->P_pad * t->K_pad));  // zero padding
+    if (sr_sample_smem(P) > (size_t)c->smem_optin)
+      return fail(MOLE_ERR_UNSUPPORTED, "too many parameters for the SR sample kernel's shared-memory sums");
+    CUDA_TRY(cudaMalloc(&t->O, sizeof(float) * (size_t)std::min(W, kCenterRows) * P));
+    CUDA_TRY(cudaMalloc(&t->center, sizeof(float) * P));
+    CUDA_TRY(cudaMalloc(&t->Ob, sizeof(__nv_bfloat16) * (size_t)t->K_cap * t->P_pad));
+    // zero padding columns (never written); rows past a launch's last sample are zeroed before it
+    CUDA_TRY(cudaMemset(t->Ob, 0, sizeof(__nv_bfloat16) * (size_t)t->K_cap * t->P_pad));
+    CUDA_TRY(cudaMalloc(&t->partial, sizeof(float) * 2 * (size_t)t->n_cta * P));
     CUDA_TRY(cudaMalloc(&t->S, sizeof(double) * (size_t)t->P_pad * t->P_pad));
     CUDA_TRY(cudaMalloc(&t->E, sizeof(double) * W));
-    CUDA_TRY(cudaMalloc(&t->center, sizeof(double) * P));
+    CUDA_TRY(cudaMalloc(&t->x, sizeof(double) * P));
     CUDA_TRY(cudaMalloc(&t->sumO, sizeof(double) * P));
     CUDA_TRY(cudaMalloc(&t->sumEO, sizeof(double) * P));
     CUDA_TRY(cudaMalloc(&t->work, sizeof(double) * (6 * (size_t)P + 8)));
     CUDA_TRY(cudaMalloc(&t->status, sizeof(int)));
     CUDA_TRY(cudaMalloc(&w->srl_eval, sizeof(double) * (size_t)W * (3 + 3 * (s->n_up + s->n_dn) + 8)));
     w->srl_map = new CUtensorMap();
-    CUDA_TRY(encode_ot_tensor_map(w->srl_map, t->Ot, t->P_pad, t->K_pad));
+    CUDA_TRY(encode_ob_tensor_map(w->srl_map, t->Ob, t->P_pad, t->K_cap));
   }
   SrLargeState* t = w->srl;
-  CUDA_TRY(cudaMemsetAsync(t->S, 0, sizeof(double) * (size_t)t->P_pad * t->P_pad, c->stream));
   CUDA_TRY(cudaMemsetAsync(t->sumO, 0, sizeof(double) * P, c->stream));
   CUDA_TRY(cudaMemsetAsync(t->sumEO, 0, sizeof(double) * P, c->stream));
   CUDA_TRY(cudaMemsetAsync(t->status, 0, sizeof(int), c->stream));
   t->count = 0.0;
   t->sumE = t->sumE2 = 0.0;
+  t->rows = 0;
   t->have_center = false;
+  t->s_stored = false;
   t->finalized = false;
+  return MOLE_OK;
+}
+
+// The samples held in Ob through the S-GEMM: S = their sum for the first
+// launch of an iteration, S += it after.
+static int srl_flush(mole_walkers* w) {
+  SrLargeState* t = w->srl;
+  mole_ctx* c = w->sys->ctx;
+  if (t->rows == 0) return MOLE_OK;
+  const int k_pad = (t->rows + kSBK - 1) / kSBK * kSBK;
+  if (k_pad > t->rows)  // rows an earlier launch used
+    CUDA_TRY(cudaMemsetAsync(t->Ob + (size_t)t->rows * t->P_pad, 0,
+                             sizeof(__nv_bfloat16) * (size_t)(k_pad - t->rows) * t->P_pad, c->stream));
+  Timer tg(c, 3);
+  CUDA_TRY(launch_s_gemm(w->srl_map, t->S, t->P_pad, k_pad, t->s_stored, t->status, c->stream));
+  tg.stop();
+  int st = 0;
+  CUDA_TRY(cudaMemcpyAsync(&st, t->status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (st & 4) return fail(MOLE_ERR_TIMEOUT, "S-matrix kernel wait timed out");
+  t->s_stored = true;
+  t->rows = 0;
+  t->gemm_launches += 1;
+  t->gemm_rows += k_pad;
   return MOLE_OK;
 }
 
@@ -1034,6 +1068,8 @@ static int srl_finalize(mole_walkers* w, double eps) {
     if (eps != t->eps) return fail(MOLE_ERR_INVALID_ARG, "S was already finalised with another shift");
     return MOLE_OK;
   }
+  const int rc = srl_flush(w);
+  if (rc) return rc;
   CUDA_TRY(launch_finalize_s(t->S, t->P, t->P_pad, t->sumO, t->count, eps, c->stream));
   t->finalized = true;
   t->eps = eps;
@@ -1083,23 +1119,32 @@ int mole_sr_collect_sample(mole_walkers* w, int32_t precision) {
   Timer tm(c, 2);
   if (precision == MOLE_PREC_MIXED) CUDA_TRY(eval32(s)(s->sp32, a, grid_for(W), c->stream));
   else CUDA_TRY(eval64(s)(s->sp64, a, grid_for(W), c->stream));
-  CUDA_TRY(launch_copy_cols(a.O, 8, nwalker_par, t->O, P, W, c->stream));
-  if (s->nn_on)
-    CUDA_TRY(launch_nn_ogen(s->sp32, w->pos, W, s->n_up, N, t->O, P, nwalker_par, std::min(W, 3 * c->n_sm),
-                            c->stream));
-  CUDA_TRY(launch_center_transpose(t->O, W, P, P, t->E, t->center, !t->have_center, t->Ot, t->K_pad, t->sumO,
-                                   t->sumEO, nullptr, c->stream));
+  if (!t->have_center) {
+    // c = the mean O_k of the first kCenterRows walkers of the iteration's
+    // first sample: S and the gradient do not depend on c (finalize_s removes
+    // the mean exactly), it only keeps the BF16 operand small
+    const int nc = std::min(W, kCenterRows);
+    CUDA_TRY(launch_copy_cols(a.O, 8, nwalker_par, t->O, P, nc, c->stream));
+    if (s->nn_on)
+      CUDA_TRY(launch_nn_ogen(s->sp32, w->pos, W, nc, s->n_up, N, t->O, P, nwalker_par, std::min(W, 3 * c->n_sm),
+                              c->stream));
+    CUDA_TRY(launch_center_rows(t->O, nc, P, P, t->center, c->stream));
+    t->have_center = true;
+  }
+  if (t->rows + W > t->K_cap) {
+    tm.stop();
+    const int rc = srl_flush(w);
+    if (rc) return rc;
+    tm = Timer(c, 2);
+  }
+  CUDA_TRY(launch_sr_sample(s->sp32, w->pos, W, s->n_up, N, s->nn_on, a.O, 8, nwalker_par, t->center, t->E,
+                            t->Ob + (size_t)t->rows * t->P_pad, t->P_pad, P, t->partial, t->n_cta, t->sumO,
+                            t->sumEO, c->stream));
   tm.stop();
-  t->have_center = true;
-  Timer tg(c, 3);
-  CUDA_TRY(launch_s_gemm(w->srl_map, t->S, t->P_pad, t->K_pad, t->status, c->stream));
-  tg.stop();
+  t->rows += W;
   std::vector<double> e(W);
   CUDA_TRY(cudaMemcpyAsync(e.data(), t->E, sizeof(double) * W, cudaMemcpyDeviceToHost, c->stream));
-  int st = 0;
-  CUDA_TRY(cudaMemcpyAsync(&st, t->status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(cudaStreamSynchronize(c->stream));
-  if (st & 4) return fail(MOLE_ERR_TIMEOUT, "S-matrix kernel wait timed out");
   for (double v : e) {
     t->sumE += v;
     t->sumE2 += v * v;
@@ -1131,7 +1176,7 @@ int mole_sr_collect_solve(mole_walkers* w, double eps, double step, int32_t max_
   const int frc = srl_finalize(w, eps);
   if (frc) return frc;
   double* d_b = t->work + 5 * (size_t)P + 8;  // scratch after the CG vectors
-  double* d_x = t->center;                     // reuse: the centre is not needed after the last sample
+  double* d_x = t->x;
   CUDA_TRY(cudaMemcpyAsync(d_b, b.data(), sizeof(double) * P, cudaMemcpyHostToDevice, c->stream));
   int iters = 0;
   double rel = 0.0;

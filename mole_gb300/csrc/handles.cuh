@@ -49,6 +49,7 @@ using namespace mole;  // the handle structs below are global (C ABI) types
 struct mole_ctx {
   int device = 0;
   int n_sm = 0;
+  int smem_optin = 0;  // shared memory a CTA may opt in to (bytes)
   cudaStream_t own = nullptr;
   cudaStream_t stream = nullptr;
   bool timing = false;

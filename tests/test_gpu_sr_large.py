@@ -35,8 +35,9 @@ def test_network_log_derivatives_match_oracle(ctx):
 
 @pytest.mark.parametrize("n_samples", [3, 6])
 def test_tensor_core_s_matrix_and_cg_solve(ctx, n_samples):
-    # 3 samples: one GEMM launch over 3 chunks at the solve; 6: a launch over
-    # 4 chunks when Ot fills (storing S), then one over 2 adding to it
+    # 3 samples: one GEMM launch over the 3 samples' rows at the solve; 6: a
+    # launch over 4 samples when the operand buffer fills (storing S), then
+    # one over 2 adding to it
     s = lih_nn(std=0.1)
     wf = api.WaveFunction(ctx, s)
     W = 512
