@@ -45,7 +45,7 @@ def parse():
     p.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "df64"])
     p.add_argument("--no-extras", action="store_true", help="skip the e2e, mixed and CPU-baseline legs")
     p.add_argument("--no-clocks", action="store_true", help="do not sample nvidia-smi during the timed region")
-    p.add_argument("--case", default=None, choices=["h2-vmc", "lih-nn-vmc", "sgemm", "be-dmc", "ragged-batch",
+    p.add_argument("--case", default=None, choices=["h2-vmc", "lih-nn-vmc", "sgemm", "be-dmc", "ragged-batch", "ragged-full",
                                                      "long-c4", "long-c5"],
                    help="run one small kernel case (for profiling) and exit")
     return p.parse_args()
@@ -115,6 +115,10 @@ def run_case(case: str, precision: str = "fp64") -> None:
     extra = {}
     if case == "long-c4":
         print(json.dumps({"case": case, **long_c4(ctx), "seconds": time.perf_counter() - t0}, default=_json_default))
+        return
+    if case == "ragged-full":
+        print(json.dumps({"case": case, **ragged_batch_leg(ctx, 5), "seconds": time.perf_counter() - t0},
+                         default=_json_default))
         return
     if case == "long-c5":
         r = dmc_leg(ctx, n_eq=2000, n_steps=20000, train_iters=40, raw_eloc_leg=True)

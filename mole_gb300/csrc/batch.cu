@@ -13,7 +13,10 @@
 namespace mole {
 
 template <class R, int MOVE>
-__global__ void __launch_bounds__(kBatchMaxThreads) batch_vmc_kernel(const BatchArgs a) {
+// 168 registers: shared memory holds about 12 warps per SM at N = 10 (520 B
+// per walker), which 168 registers per thread also allow; below that the
+// kernel spills.
+__global__ void __maxnreg__(168) batch_vmc_kernel(const BatchArgs a) {
   auto* sp = reinterpret_cast<SysParams<R>*>(mole_dyn_smem);
   double* st = reinterpret_cast<double*>(mole_dyn_smem + batch_sp_bytes<R>());
   double* red = st + (size_t)a.slots * blockDim.x;
