@@ -45,7 +45,7 @@ def parse():
     p.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "df64"])
     p.add_argument("--no-extras", action="store_true", help="skip the e2e, mixed and CPU-baseline legs")
     p.add_argument("--no-clocks", action="store_true", help="do not sample nvidia-smi during the timed region")
-    p.add_argument("--case", default=None, choices=["h2-vmc", "lih-nn-vmc", "sgemm", "be-dmc", "ragged-batch", "ragged-full",
+    p.add_argument("--case", default=None, choices=["h2-vmc", "lih-nn-vmc", "sgemm", "be-dmc", "ragged-batch", "ragged-full", "he-c1",
                                                      "long-c4", "long-c5"],
                    help="run one small kernel case (for profiling) and exit")
     return p.parse_args()
@@ -115,6 +115,21 @@ def run_case(case: str, precision: str = "fp64") -> None:
     extra = {}
     if case == "long-c4":
         print(json.dumps({"case": case, **long_c4(ctx), "seconds": time.perf_counter() - t0}, default=_json_default))
+        return
+    if case == "he-c1":
+        # the helium singlet's FP64 run at full size (the small-ensemble team kernel)
+        wf = api.WaveFunction(ctx, S.helium(1.6875, 0.3))
+        wk = api.Walkers(wf, 1024, seed=0x5EED)
+        samp = api.Sampler(wf, api.MetropolisBox(0.5), wk, precision=api.PREC_FP64)
+        samp.run(10, 0, 1)
+        wk.init()
+        wk.step = 0
+        ctx.enable_timing(True)
+        r = samp.run(1000, 10000, 100)
+        ms, n = ctx.kernel_time(0)
+        ctx.enable_timing(False)
+        print(json.dumps({"case": case, "energy": r.energy, "error": r.error, "kernel_ms": ms, "launches": n,
+                          "walker_steps_per_s": 1024 * 11000 / (ms * 1e-3)}))
         return
     if case == "ragged-full":
         print(json.dumps({"case": case, **ragged_batch_leg(ctx, 5), "seconds": time.perf_counter() - t0},

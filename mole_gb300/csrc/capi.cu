@@ -74,7 +74,7 @@ MOLE_DECL_DF(1, 1)
 MOLE_DECL_DF(2, 1)
 MOLE_DECL_DF(2, 2)
 KernelSetT<double>::Vmc compact_vmc64(int nu, int nd, int slot);
-KernelSetT<double>::Vmc team_vmc64(int nu, int nd, int slot);
+KernelSetT<double>::Vmc team_vmc64(int nu, int nd, int slot, int n_nuc);
 const NnKernelSetT<double>* nn_kernels_f64_2_2();
 const NnKernelSetT<float>* nn_kernels_f32_2_2();
 
@@ -260,11 +260,16 @@ KernelSetT<double>::Vmc vmc64_compact(const mole_system* s, int slot, int drift,
   if (!one_electron_per_spin_1s(s, drift) || n_sm <= 0 || W < n_sm * kCompactBlock) return nullptr;
   return compact_vmc64(s->n_up, s->n_dn, slot);
 }
-// The same systems on small ensembles (up to two 32-walker teams per SM):
-// the three-warp teams of team.cuh.
+// The same systems on small ensembles (up to two 32-walker teams per SM),
+// with one 1s function on each of at most two nuclei: the three-warp teams
+// of team.cuh.
 KernelSetT<double>::Vmc vmc64_team(const mole_system* s, int slot, int drift, int W, int n_sm) {
   if (!one_electron_per_spin_1s(s, drift) || n_sm <= 0 || W > 2 * 32 * n_sm) return nullptr;
-  return team_vmc64(s->n_up, s->n_dn, slot);
+  const SysParams<double>& sp = s->sp64;
+  if (sp.n_nuc < 1 || sp.n_nuc > 2 || sp.n_basis != sp.n_nuc) return nullptr;
+  for (int I = 0; I <= sp.n_nuc; ++I)
+    if (sp.nuc_b0[I] != I) return nullptr;
+  return team_vmc64(s->n_up, s->n_dn, slot, sp.n_nuc);
 }
 KernelSetT<double>::Eval eval64(const mole_system* s) { return s->nn_on ? s->nk64->eval : s->k64->eval[s->en_on]; }
 KernelSetT<float>::Eval eval32(const mole_system* s) { return s->nn_on ? s->nk32->eval : s->k32->eval[s->en_on]; }
