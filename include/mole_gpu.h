@@ -269,10 +269,16 @@ int mole_sr_update(mole_ctx* ctx, int32_t P, double count, const double* sum_E, 
  * replaces StochasticReconfiguration::construct_sr_matrix and the solveh call
  * (src/optimize/src/optimizers.rs:191-252) when P is too large for per-walker
  * sums. Each sample takes O_k = d ln psi / d theta_k and E_L of every walker at
- * its current position (move the walkers with mole_vmc_run in between), centres
- * O on the first sample's mean c, and accumulates S = sum (O-c)(O-c)^T on the
- * tensor cores (BF16 operands, FP32 accumulation inside a 128 x 128 tile, FP64
- * across tiles and samples). mole_sr_collect_solve forms
+ * its current position (move the walkers with mole_vmc_run in between) and
+ * writes each walker's row bf16(O - c) of the S-GEMM's operand, c being the
+ * mean O_k of the first 1,024 walkers of the first sample after
+ * mole_sr_collect_begin; the sums of O - c and E (O - c) are kept in FP32
+ * within a CTA and FP64 across CTAs. S = sum (O-c)(O-c)^T is accumulated on
+ * the tensor cores (BF16 operands, FP32 accumulation inside a 128 x 128 tile,
+ * FP64 across launches) once per four samples (fewer when four would exceed
+ * 8 GiB of operand rows): when a sample does not fit, and at
+ * mole_sr_collect_solve / mole_sr_collect_matrix. S and g do not depend on c.
+ * mole_sr_collect_solve forms
  * S_kl = <(O-c)_k (O-c)_l> - <O-c>_k <O-c>_l + eps delta_kl and
  * g_k = 2 (<E O_k> - <E><O_k>) and solves S x = -g/2 in FP64 by
  * Jacobi-preconditioned conjugate gradients (max_iter, relative residual tol;
