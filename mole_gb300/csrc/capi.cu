@@ -1004,7 +1004,7 @@ int mole_sr_collect_begin(mole_walkers* w) {
     auto t = new SrLargeState();
     std::memset(t, 0, sizeof(*t));
     t->P = P;
-    t->P_pad = (P + kSBM - 1) / kSBM * kSBM;
+    t->P_pad = (P + kSBN - 1) / kSBN * kSBN;
     const size_t sample_bytes = sizeof(__nv_bfloat16) * (size_t)W * t->P_pad;
     const int n_samples = (int)std::max<size_t>(1, std::min<size_t>(kObSamples, kObBudget / sample_bytes));
     t->K_cap = (n_samples * W + kSBK - 1) / kSBK * kSBK;

@@ -606,9 +606,9 @@ __device__ __forceinline__ uint64_t umma_desc_mn_sw128(uint32_t saddr) {
 }
 
 // Instruction descriptor of kind::f16: BF16 A and B, FP32 accumulator,
-// both MN-major (bits 15 and 16), M = 128, N = 128.
+// both MN-major (bits 15 and 16), M = 128, N = 256.
 constexpr uint32_t kSIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) |
-                             ((uint32_t)(kSBM >> 3) << 17) | ((uint32_t)(kSBM >> 4) << 24);
+                             ((uint32_t)(kSBN >> 3) << 17) | ((uint32_t)(kSBM >> 4) << 24);
 
 __device__ __forceinline__ void umma_f16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
   asm volatile(
@@ -621,48 +621,57 @@ __device__ __forceinline__ void umma_commit(uint64_t* bar) {
                : "memory");
 }
 
-// S[ti][tj] (+)= sum_k Ob[k][ti tile]^T Ob[k][tj tile] over the upper 128 x
-// 128 tiles, K = K_pad rows of Ob; `accumulate` adds to S, else stores.
-__global__ void __launch_bounds__(128, 2) s_gemm_kernel(const __grid_constant__ CUtensorMap tmap, double* S, int P_pad,
+// Tiles of S: row tile ti (128 parameters) against column block tb (256
+// parameters), for the blocks that reach the upper triangle (tb >= ti / 2;
+// an odd row tile's first block also covers the tile left of its diagonal,
+// which finalize_s overwrites from the upper one).
+__host__ __device__ inline int s_gemm_tiles(int P_pad) {
+  const int T = P_pad / kSBM, TB = P_pad / kSBN;
+  int n = 0;
+  for (int ti = 0; ti < T; ++ti) n += TB - ti / 2;
+  return n;
+}
+
+// S[ti][tb] (+)= sum_k Ob[k][ti tile]^T Ob[k][tb block] over K = K_pad rows
+// of Ob; `accumulate` adds to S, else stores. One CTA per SM: four 48 KB
+// pipeline stages (A 16 KB + B 32 KB), 256 TMEM columns.
+__global__ void __launch_bounds__(128, 1) s_gemm_kernel(const __grid_constant__ CUtensorMap tmap, double* S, int P_pad,
                                                         int K_pad, int accumulate, int* status) {
   extern __shared__ __align__(1024) unsigned char gemm_smem[];
   const uintptr_t base = ((uintptr_t)gemm_smem + 1023) & ~(uintptr_t)1023;
   unsigned char* tiles = (unsigned char*)base;  // [stage][A | B]
-  uint64_t* full = (uint64_t*)(tiles + 2 * kSStages * kSTileBytes);
+  uint64_t* full = (uint64_t*)(tiles + kSStages * kSStageBytes);
   uint64_t* empty = full + kSStages;
   uint64_t* done = empty + kSStages;
   uint32_t* tmem_slot = (uint32_t*)(done + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-  // upper-triangular tile (ti <= tj) of this CTA, in bands of kSBand tile
-  // rows walked column by column: CTAs running together share B panels, and
-  // a band's A panels stay in L2 while its columns stream past
-  const int T = P_pad / kSBM;
-  int ti = 0, tj = 0;
+  // this CTA's tile, in bands of kSBand row tiles walked column block by
+  // column block: CTAs running together share the band's row panels and
+  // each column panel
+  const int T = P_pad / kSBM, TB = P_pad / kSBN;
+  int ti = 0, tb = 0;
   {
     int rem = blockIdx.x;
-    for (int r0 = 0; r0 < T; r0 += kSBand) {
+    bool found = false;
+    for (int r0 = 0; r0 < T && !found; r0 += kSBand) {
       const int r1 = min(r0 + kSBand, T);
-      const int tri = (r1 - r0) * (r1 - r0 + 1) / 2;  // columns r0..r1-1 (diagonal part)
-      const int band = tri + (T - r1) * (r1 - r0);
+      int band = 0;
+      for (int r = r0; r < r1; ++r) band += TB - r / 2;
       if (rem >= band) {
         rem -= band;
         continue;
       }
-      if (rem < tri) {
-        int c = 0;
-        while (rem >= c + 1) {
-          rem -= c + 1;
-          ++c;
+      for (int c = r0 / 2; c < TB; ++c) {
+        const int n = min(r1, 2 * c + 2) - r0;  // rows of the band that reach column block c
+        if (rem < n) {
+          ti = r0 + rem;
+          tb = c;
+          found = true;
+          break;
         }
-        tj = r0 + c;
-        ti = r0 + rem;
-      } else {
-        rem -= tri;
-        tj = r1 + rem / (r1 - r0);
-        ti = r0 + rem % (r1 - r0);
+        rem -= n;
       }
-      break;
     }
   }
 
@@ -676,7 +685,7 @@ __global__ void __launch_bounds__(128, 2) s_gemm_kernel(const __grid_constant__ 
   }
   if (warp == 2) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(128u));
+                 "r"((uint32_t)kSBN));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
@@ -691,12 +700,13 @@ __global__ void __launch_bounds__(128, 2) s_gemm_kernel(const __grid_constant__ 
       const int s = kb % kSStages;
       if (kb >= kSStages) ok = mbar_wait(&empty[s], ((kb / kSStages) - 1) & 1);
       if (!ok) break;
-      mbar_expect_tx(&full[s], 2 * kSTileBytes);
-      unsigned char* a = tiles + (2 * s) * kSTileBytes;
-      tma_load_2d(a, &tmap, ti * kSBM, kb * kSBK, &full[s]);
-      tma_load_2d(a + kSBoxBytes, &tmap, ti * kSBM + 64, kb * kSBK, &full[s]);
-      tma_load_2d(a + kSTileBytes, &tmap, tj * kSBM, kb * kSBK, &full[s]);
-      tma_load_2d(a + kSTileBytes + kSBoxBytes, &tmap, tj * kSBM + 64, kb * kSBK, &full[s]);
+      mbar_expect_tx(&full[s], kSStageBytes);
+      unsigned char* a = tiles + s * kSStageBytes;
+      unsigned char* bt = a + kSATileBytes;
+#pragma unroll
+      for (int q = 0; q < kSBM / 64; ++q) tma_load_2d(a + q * kSBoxBytes, &tmap, ti * kSBM + 64 * q, kb * kSBK, &full[s]);
+#pragma unroll
+      for (int q = 0; q < kSBN / 64; ++q) tma_load_2d(bt + q * kSBoxBytes, &tmap, tb * kSBN + 64 * q, kb * kSBK, &full[s]);
     }
   } else if (warp == 1 && lane == 0) {
     for (int kb = 0; kb < nk && ok; ++kb) {
@@ -704,8 +714,8 @@ __global__ void __launch_bounds__(128, 2) s_gemm_kernel(const __grid_constant__ 
       ok = mbar_wait(&full[s], (kb / kSStages) & 1);
       if (!ok) break;
       asm volatile("tcgen05.fence::after_thread_sync;");
-      const uint32_t a0 = smem_u32(tiles + (2 * s) * kSTileBytes);
-      const uint32_t b0 = smem_u32(tiles + (2 * s + 1) * kSTileBytes);
+      const uint32_t a0 = smem_u32(tiles + s * kSStageBytes);
+      const uint32_t b0 = a0 + kSATileBytes;
 #pragma unroll
       for (int kk = 0; kk < kSBK / 16; ++kk)  // 16 samples = two swizzle atoms = 2,048 bytes
         umma_f16(tmem, umma_desc_mn_sw128(a0 + kk * 2048), umma_desc_mn_sw128(b0 + kk * 2048), kSIdesc,
@@ -717,7 +727,7 @@ __global__ void __launch_bounds__(128, 2) s_gemm_kernel(const __grid_constant__ 
   __syncwarp();
   // epilogue: thread (warp, lane) reads row 32 warp + lane of the tile from
   // TMEM, 16 columns at a time, into a shared staging tile (the pipeline's
-  // buffers, idle once `done` has fired); the warp then adds its 32 rows to
+  // buffers, idle once `done` has fired); the warp then writes its 32 rows of
   // S two rows per instruction, 16 consecutive doubles per half-warp
   const bool got = mbar_wait(done, 0);
   if (!ok || !got) {
@@ -726,10 +736,9 @@ __global__ void __launch_bounds__(128, 2) s_gemm_kernel(const __grid_constant__ 
     asm volatile("tcgen05.fence::after_thread_sync;");
     constexpr int LD = 17;  // staging row stride (doubles), odd: conflict-free columns
     double* stage = reinterpret_cast<double*>(tiles) + (size_t)warp * 32 * LD;
-    const int row = warp * 32 + lane;
     const int half = lane >> 4, col = lane & 15;
 #pragma unroll 1
-    for (int c0 = 0; c0 < kSBM; c0 += 16) {
+    for (int c0 = 0; c0 < kSBN; c0 += 16) {
       uint32_t v[16];
       const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
       asm volatile(
@@ -742,7 +751,7 @@ __global__ void __launch_bounds__(128, 2) s_gemm_kernel(const __grid_constant__ 
 #pragma unroll
       for (int i = 0; i < 16; ++i) stage[lane * LD + i] = (double)__uint_as_float(v[i]);
       __syncwarp();
-      double* out0 = S + (size_t)(ti * kSBM + warp * 32 + half) * P_pad + tj * kSBM + c0 + col;
+      double* out0 = S + (size_t)(ti * kSBM + warp * 32 + half) * P_pad + tb * kSBN + c0 + col;
       if (accumulate) {
         // all 16 loads of the chunk in flight before the first store
         double old[16];
@@ -756,21 +765,18 @@ __global__ void __launch_bounds__(128, 2) s_gemm_kernel(const __grid_constant__ 
       }
       __syncwarp();
     }
-    (void)row;
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
-  if (warp == 2) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(128u));
+  if (warp == 2) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)kSBN));
 }
 
 cudaError_t launch_s_gemm(const CUtensorMap* tmap, double* S, int P_pad, int K_pad, bool accumulate, int* status,
                           cudaStream_t s) {
-  if (P_pad % kSBM || K_pad % kSBK || K_pad <= 0) return cudaErrorInvalidValue;
-  const int T = P_pad / kSBM;
-  const int tiles = T * (T + 1) / 2;
+  if (P_pad % kSBN || K_pad % kSBK || K_pad <= 0) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(s_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSGemmSmem);
   if (e != cudaSuccess) return e;
-  s_gemm_kernel<<<tiles, 128, kSGemmSmem, s>>>(*tmap, S, P_pad, K_pad, accumulate ? 1 : 0, status);
+  s_gemm_kernel<<<s_gemm_tiles(P_pad), 128, kSGemmSmem, s>>>(*tmap, S, P_pad, K_pad, accumulate ? 1 : 0, status);
   return cudaGetLastError();
 }
 
@@ -789,7 +795,7 @@ cudaError_t encode_ob_tensor_map(CUtensorMap* tmap, __nv_bfloat16* Ob, int P_pad
     if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p) return cudaErrorNotSupported;
     fn = (EncodeTiledFn)p;
   }
-  if (P_pad % kSBM || K_rows % kSBK) return cudaErrorInvalidValue;
+  if (P_pad % kSBN || K_rows % kSBK) return cudaErrorInvalidValue;
   const cuuint64_t dims[2] = {(cuuint64_t)P_pad, (cuuint64_t)K_rows};
   const cuuint64_t strides[1] = {(cuuint64_t)P_pad * sizeof(__nv_bfloat16)};
   const cuuint32_t box[2] = {64u, (cuuint32_t)kSBK};

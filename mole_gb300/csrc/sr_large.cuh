@@ -11,14 +11,16 @@
 
 namespace mole {
 
-// S-matrix tiles: 128 x 128 parameters, 64 samples per pipeline stage.
-constexpr int kSBM = 128;
+// S-matrix tiles: 128 x 256 parameters, 64 samples per pipeline stage.
+constexpr int kSBM = 128;  // rows of a tile (M)
+constexpr int kSBN = 256;  // columns of a tile (N)
 constexpr int kSBK = 64;
-constexpr int kSStages = 3;  // 97 KB of stages: two CTAs per SM, one's epilogue under the other's MMAs
-constexpr int kSBand = 16;  // tile rows per band of the tile order
-constexpr uint32_t kSTileBytes = kSBM * kSBK * 2;  // one BF16 operand tile, 16 KB (two 64 x 64 boxes)
-constexpr uint32_t kSBoxBytes = 64 * kSBK * 2;     // one TMA box, 8 KB
-constexpr size_t kSGemmSmem = 2 * kSStages * (size_t)kSTileBytes + 1024 + 256;
+constexpr int kSStages = 4;  // 4 x 48 KB: one CTA per SM
+constexpr int kSBand = 16;   // row tiles per band of the tile order
+constexpr uint32_t kSBoxBytes = 64 * kSBK * 2;               // one TMA box, 8 KB
+constexpr uint32_t kSATileBytes = kSBM * kSBK * 2;           // A: two boxes, 16 KB
+constexpr uint32_t kSStageBytes = (kSBM + kSBN) * kSBK * 2;  // A + B (four boxes), 48 KB
+constexpr size_t kSGemmSmem = kSStages * (size_t)kSStageBytes + 1024 + 256;
 
 // Walkers of the first sample of an iteration whose mean O_k is the centre c.
 constexpr int kCenterRows = 1024;
@@ -29,7 +31,7 @@ constexpr size_t kObBudget = (size_t)8 << 30;
 
 struct SrLargeState {
   int P;          // parameters
-  int P_pad;      // columns of Ob, a multiple of 128
+  int P_pad;      // columns of Ob, a multiple of 256
   int K_cap;      // rows of Ob: whole samples, rounded up to a multiple of 64
   int rows;       // rows of Ob holding samples not yet added into S
   int n_cta;      // CTAs of the sample kernel (rows of `partial`)
