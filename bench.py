@@ -161,11 +161,15 @@ def run_case(case: str, precision: str = "fp64") -> None:
                 wk.sr_collect_begin()
                 for _ in range(4):
                     wk.sr_collect_sample(api.PREC_MIXED)
-                wk.sr_collect_solve(1e-3, 0.05)
+                torch.cuda.synchronize()
+                ts = time.perf_counter()
+                _, _, info = wk.sr_collect_solve(1e-3, 0.05)
+                solve_s = time.perf_counter() - ts
             s_ms, s_n = ctx.kernel_time(2)
             g_ms, g_n = ctx.kernel_time(3)
             ctx.enable_timing(False)
-            extra = {"sample_ms": s_ms / max(s_n, 1), "s_gemm_ms_per_launch": g_ms / max(g_n, 1)}
+            extra = {"sample_ms": s_ms / max(s_n, 1), "s_gemm_ms_per_launch": g_ms / max(g_n, 1),
+                     "solve_ms": 1e3 * solve_s, "solve_iterations": int(info[2]), "solve_rel_residual": info[3]}
             r = None
     elif case == "ragged-batch":
         systems, walkers, widths = api.ragged_batch(64, w_range=(256, 1024))
