@@ -1,0 +1,40 @@
+"""The three-warp team kernel (small ensembles of one-electron-per-spin 1s
+systems) against the one-walker-per-thread FP64 kernel.
+
+A walker's random stream depends only on the seed and the walker's index, so
+walkers 0..255 of a 256-walker run (team kernel) and of a 12,000-walker run
+(the per-thread kernel: too many walkers for teams, too few for the packed
+kernel) started from the same positions follow the same trajectory. The team
+kernel computes the same operations on the same operands, so the positions
+must agree bit for bit, with one nucleus (He) and two (H2), with and without
+the SR sums."""
+import numpy as np
+import pytest
+
+from mole_gb300 import api
+from mole_gb300 import system as S
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name,move,step,sr", [
+    ("He", 0, 0.5, False),
+    ("He", 0, 0.5, True),
+    ("H2", 1, 0.4, False),
+    ("H2", 1, 0.4, True),
+])
+def test_team_trajectories_equal_the_per_thread_kernel(ctx, name, move, step, sr):
+    s = {"He": S.helium(1.6875, 0.3), "H2": S.h2(1.0, 0.5)}[name]
+    wf = api.WaveFunction(ctx, s)
+    n_small, n_large = 256, 12000
+    pos = np.random.default_rng(11).normal(size=(n_large, s.n_elec, 3))
+    out = {}
+    for W in (n_small, n_large):
+        wk = api.Walkers(wf, W, seed=0x5EED + 40)
+        wk.set_positions(pos[:W])
+        mv = api.MetropolisBox(step) if move == 0 else api.MetropolisGaussian(step)
+        r = api.Sampler(wf, mv, wk, precision=api.PREC_FP64).run(3, 120, 10, sr=sr)
+        out[W] = (wk.positions()[:n_small], r)
+        wk.close()
+    np.testing.assert_array_equal(out[n_small][0], out[n_large][0])
+    assert out[n_small][1].acceptance > 0.3
