@@ -12,16 +12,11 @@
 // spin-block sizes are runtime values (nu, nd <= 5), so the walker state sits
 // in shared memory, walker-fastest: slot k of thread t is st[k * blockDim + t]
 // (a warp touches 32 consecutive doubles: no bank conflicts). A walker keeps
-// only what is expensive to rebuild -- its positions and the two inverse
-// Slater matrices; orbital, Jastrow and potential terms are re-evaluated in
-// the arithmetic type R (FP32 in the mixed form) when needed. The inverse,
-// the Sherman-Morrison ratio and update and the local-energy assembly are
-// FP64 in the FP64 form and double-float (df64.cuh: about 48 significant
-// bits, FP32 exponent range) in the FP32 form, whose FP64 pipe then carries
-// only the inverse's periodic rebuild and the energy sums: GB300 issues one
-// FP64 warp instruction per 64 cycles per sub-partition whatever the number
-// of active lanes, so with the inverse in FP64 the FP32 form was bound by
-// its FP64 instructions.
+// only what is expensive to rebuild in FP64 -- its positions and the two
+// inverse Slater matrices; orbital, Jastrow and potential terms are
+// re-evaluated in the arithmetic type R (FP32 in the mixed form) when needed.
+// The inverse, the Sherman-Morrison ratio and update, the local-energy
+// assembly and every accumulation stay FP64 in both forms.
 #pragma once
 
 #include "kernels.cuh"
@@ -100,19 +95,6 @@ __device__ __forceinline__ R div_t(R a, R b) {
   else return __fdividef(a, b);
 }
 
-// Element type of the inverse: FP64 in the FP64 form, double-float in the
-// FP32 form (the same 8 bytes of shared memory).
-template <class R>
-using BatchInv = std::conditional_t<sizeof(R) == sizeof(double), double, df64>;
-
-// acc + x b in the inverse's type (x an orbital term in R): one contracted
-// FP64 multiply-add, or a double-float add of the exactly split product.
-template <class R>
-__device__ __forceinline__ double inv_madd(double acc, R x, double b) {
-  return acc + up_d<R>(x) * b;
-}
-__device__ __forceinline__ df64 inv_madd(df64 acc, float x, df64 b) { return acc + df_mul(b, x); }
-
 // Orbital values of spin block `spin` at r (the first kMaxSpin orbitals; the
 // unused ones have zero coefficients) and the e-n Jastrow value.
 template <class R>
@@ -181,8 +163,8 @@ struct BatchWalker {
   double* X;   // X[(3e + c) * xs]: the FP64 positions the moves accumulate into
                // (shared slots in the FP64 form, the global SoA buffer in the FP32 form)
   R* Xr;       // the positions in the arithmetic type (X itself when R is double)
-  BatchInv<R>* Bu;  // inverse of the up Slater matrix, Bu[(k * nu + j) * nt]
-  BatchInv<R>* Bd;  // inverse of the down Slater matrix
+  double* Bu;  // inverse of the up Slater matrix, Bu[(k * nu + j) * nt]
+  double* Bd;  // inverse of the down Slater matrix
   int nt, xs, nu, nd;
   __device__ __forceinline__ double& x(int e, int c) const { return X[(size_t)(3 * e + c) * xs]; }
   __device__ __forceinline__ R xr(int e, int c) const { return Xr[(3 * e + c) * nt]; }
@@ -190,13 +172,12 @@ struct BatchWalker {
     X[(size_t)(3 * e + c) * xs] = v;
     if constexpr (sizeof(R) != sizeof(double)) Xr[(3 * e + c) * nt] = (R)v;
   }
-  __device__ __forceinline__ BatchInv<R>* B(int spin) const { return spin ? Bd : Bu; }
+  __device__ __forceinline__ double* B(int spin) const { return spin ? Bd : Bu; }
 };
 
 // Rebuilds both inverses in FP64 from fresh orbital values by Gauss-Jordan
 // elimination with partial pivoting (the matrix in registers, padded to
-// kMaxSpin x kMaxSpin; the inverse built in place in the shared slots, as
-// FP64, then split into double-float pairs in the FP32 form).
+// kMaxSpin x kMaxSpin; the inverse written straight to the shared slots).
 template <class R>
 __device__ bool batch_refresh(const SysParams<R>& sp, const BatchWalker<R>& wk) {
   bool ok = true;
@@ -204,7 +185,7 @@ __device__ bool batch_refresh(const SysParams<R>& sp, const BatchWalker<R>& wk) 
     const int n = spin ? wk.nd : wk.nu;
     if (n == 0) continue;
     const int e0 = spin ? wk.nu : 0;
-    double* inv = reinterpret_cast<double*>(wk.B(spin));
+    double* inv = wk.B(spin);
     const int nt = wk.nt;
     double a[kMaxSpin][kMaxSpin];
 #pragma unroll
@@ -263,13 +244,6 @@ __device__ bool batch_refresh(const SysParams<R>& sp, const BatchWalker<R>& wk) 
         for (int j = 0; j < n; ++j) inv[(r * n + j) * nt] -= f * inv[(col * n + j) * nt];
       }
     }
-    if constexpr (sizeof(R) != sizeof(double))
-      for (int q = 0; q < n * n; ++q) {
-        // h = the top 24 bits, l = the rest (d - h is exact), renormalised
-        const double d = inv[q * nt];
-        const float h = d2f_rz(d);
-        reinterpret_cast<df64*>(inv)[q * nt] = df_fast_two_sum(h, d2f_rz(d - f2d(h)));
-      }
   }
   return ok;
 }
@@ -283,8 +257,7 @@ __device__ __forceinline__ int batch_move(const SysParams<R>& sp, const BatchWal
   const int spin = e < wk.nu ? 0 : 1;
   const int n = spin ? wk.nd : wk.nu;
   const int i = spin ? e - wk.nu : e;
-  using Bt = BatchInv<R>;
-  const Bt* B = wk.B(spin);
+  const double* B = wk.B(spin);
   const int nt = wk.nt;
 
   constexpr bool F64 = sizeof(R) == sizeof(double);
@@ -337,10 +310,10 @@ __device__ __forceinline__ int batch_move(const SysParams<R>& sp, const BatchWal
   R phi[kMaxSpin], jn;
   batch_orbitals<R>(sp, spin, rn, phi, jn);
   const R jo = sp.en_on ? batch_jen<R>(sp, ro) : (R)0;
-  Bt ratio = Bt(0);
+  double ratio = 0.0;
 #pragma unroll
   for (int k = 0; k < kMaxSpin; ++k)
-    if (k < n) ratio = inv_madd(ratio, phi[k], B[(k * n + i) * nt]);
+    if (k < n) ratio += up_d<R>(phi[k]) * B[(k * n + i) * nt];
   R dJ = jn - jo;
   for (int j = 0; j < N; ++j) {
     if (j == e) continue;
@@ -352,7 +325,7 @@ __device__ __forceinline__ int batch_move(const SysParams<R>& sp, const BatchWal
   if constexpr (F64) {
     if (!metropolis_accept(ratio, 2.0 * dJ, ubits)) return 0;
   } else {
-    const float rf = ratio.h;  // the acceptance test itself is a random comparison: FP32
+    const float rf = d2f_rz(ratio);  // the acceptance test itself is a random comparison: FP32
     if (!(rf * rf * __expf(2.0f * dJ) > uacc)) return 0;
   }
 
@@ -364,21 +337,18 @@ __device__ __forceinline__ int batch_move(const SysParams<R>& sp, const BatchWal
 #pragma unroll
     for (int c = 0; c < 3; ++c) wk.set_x(e, c, xn[c] + up_d<R>(dx[c]));
   }
-  Bt v[kMaxSpin], col[kMaxSpin];
-  Bt* Bw = wk.B(spin);
+  double v[kMaxSpin], col[kMaxSpin];
+  double* Bw = wk.B(spin);
 #pragma unroll
   for (int j = 0; j < kMaxSpin; ++j) {
     if (j >= n) break;
-    Bt s = Bt(0);
+    double s = 0.0;
 #pragma unroll
     for (int k = 0; k < kMaxSpin; ++k)
-      if (k < n) s = inv_madd(s, phi[k], Bw[(k * n + j) * nt]);
-    if constexpr (F64) v[j] = s - (j == i ? 1.0 : 0.0);
-    else v[j] = j == i ? s - df64(1.0f) : s;
+      if (k < n) s += up_d<R>(phi[k]) * Bw[(k * n + j) * nt];
+    v[j] = s - (j == i ? 1.0 : 0.0);
   }
-  Bt ir;
-  if constexpr (F64) ir = 1.0 / ratio;
-  else ir = df_rcp(ratio);
+  const double ir = 1.0 / ratio;
 #pragma unroll
   for (int k = 0; k < kMaxSpin; ++k)
     if (k < n) col[k] = Bw[(k * n + i) * nt] * ir;
@@ -387,10 +357,7 @@ __device__ __forceinline__ int batch_move(const SysParams<R>& sp, const BatchWal
     if (k >= n) break;
 #pragma unroll
     for (int j = 0; j < kMaxSpin; ++j)
-      if (j < n) {
-        if constexpr (F64) Bw[(k * n + j) * nt] -= col[k] * v[j];
-        else Bw[(k * n + j) * nt] = Bw[(k * n + j) * nt] - col[k] * v[j];
-      }
+      if (j < n) Bw[(k * n + j) * nt] -= col[k] * v[j];
   }
   return 1;
 }
@@ -402,26 +369,24 @@ template <class R>
 __device__ double batch_local_energy(const SysParams<R>& sp, const BatchWalker<R>& wk) {
   const int N = wk.nu + wk.nd;
   const int nt = wk.nt;
-  constexpr bool F64 = sizeof(R) == sizeof(double);
-  using Bt = BatchInv<R>;
-  Bt lap = Bt(0), V = Bt(sp.vnn);
+  double lap = 0.0, V = sp.vnn;
   for (int e = 0; e < N; ++e) {
     const int spin = e < wk.nu ? 0 : 1;
     const int n = spin ? wk.nd : wk.nu;
     const int i = spin ? e - wk.nu : e;
-    const Bt* B = wk.B(spin);
+    const double* B = wk.B(spin);
     const R r[3] = {wk.xr(e, 0), wk.xr(e, 1), wk.xr(e, 2)};
     OneBody<R, kMaxSpin, 0> o;
     one_body<R, kMaxSpin, 0, true, false>(sp, spin, r, o);
-    Bt gD[3] = {Bt(0), Bt(0), Bt(0)}, lD = Bt(0);
+    double gD[3] = {0.0, 0.0, 0.0}, lD = 0.0;
 #pragma unroll
     for (int k = 0; k < kMaxSpin; ++k)
       if (k < n) {
-        const Bt b = B[(k * n + i) * nt];
-        gD[0] = inv_madd(gD[0], o.grad[k][0], b);
-        gD[1] = inv_madd(gD[1], o.grad[k][1], b);
-        gD[2] = inv_madd(gD[2], o.grad[k][2], b);
-        lD = inv_madd(lD, o.lap[k], b);
+        const double b = B[(k * n + i) * nt];
+        gD[0] += up_d<R>(o.grad[k][0]) * b;
+        gD[1] += up_d<R>(o.grad[k][1]) * b;
+        gD[2] += up_d<R>(o.grad[k][2]) * b;
+        lD += up_d<R>(o.lap[k]) * b;
       }
     R gJ[3] = {o.gjen[0], o.gjen[1], o.gjen[2]};
     R lJ = o.ljen, Ve = o.ven;
@@ -438,21 +403,11 @@ __device__ double batch_local_energy(const SysParams<R>& sp, const BatchWalker<R
     }
     // the electron's Jastrow-only terms in R, the determinant terms in FP64
     const R jj = lJ + gJ[0] * gJ[0] + gJ[1] * gJ[1] + gJ[2] * gJ[2];
-    if constexpr (F64) {
-      const double dot = gD[0] * up_d<R>(gJ[0]) + gD[1] * up_d<R>(gJ[1]) + gD[2] * up_d<R>(gJ[2]);
-      lap += lD + up_d<R>(jj) + 2.0 * dot;
-      V += up_d<R>(Ve);
-    } else {
-      const df64 dot = df_mul(gD[0], gJ[0]) + df_mul(gD[1], gJ[1]) + df_mul(gD[2], gJ[2]);
-      lap = lap + (lD + df64(jj) + df_scale(dot, 2.f));
-      V = V + df64(Ve);
-    }
+    const double dot = gD[0] * up_d<R>(gJ[0]) + gD[1] * up_d<R>(gJ[1]) + gD[2] * up_d<R>(gJ[2]);
+    lap += lD + up_d<R>(jj) + 2.0 * dot;
+    V += up_d<R>(Ve);
   }
-  if constexpr (F64) return -0.5 * lap + V;
-  else {
-    const df64 E = df_scale(lap, -0.5f) + V;
-    return f2d(E.h) + f2d(E.l);
-  }
+  return -0.5 * lap + V;
 }
 
 // One work item: walkers [w0, w0 + blockDim.x) of one system, all sweeps of
@@ -478,7 +433,7 @@ __device__ void batch_item(const SysParams<R>& sp, const BatchSystem& bs, int id
   } else {
     wk.X = gp + (active ? w : 0);
     wk.xs = bs.W;
-    wk.Bu = reinterpret_cast<BatchInv<R>*>(st) + tid;
+    wk.Bu = st + tid;
     wk.Xr = reinterpret_cast<R*>(st + (size_t)a.slots * nt + (size_t)kNMom * (nt / 32)) + tid;
   }
   wk.Bd = wk.Bu + (size_t)bs.nu * bs.nu * nt;
