@@ -35,7 +35,14 @@ __global__ void __maxnreg__(168) batch_vmc_kernel(const BatchArgs a) {
     unsigned long long* dst = reinterpret_cast<unsigned long long*>(sp);
     for (int k = threadIdx.x; k < (int)(sizeof(SysParams<R>) / 8); k += blockDim.x) dst[k] = src[k];
     __syncthreads();
-    batch_item<R, MOVE>(*sp, a.info[it.x], id, it.y, st, red, a, t0);
+    const BatchSystem& bs = a.info[it.x];
+    switch (bs.nu > bs.nd ? bs.nu : bs.nd) {
+      case 1: batch_item<R, MOVE, 1>(*sp, bs, id, it.y, st, red, a, t0); break;
+      case 2: batch_item<R, MOVE, 2>(*sp, bs, id, it.y, st, red, a, t0); break;
+      case 3: batch_item<R, MOVE, 3>(*sp, bs, id, it.y, st, red, a, t0); break;
+      case 4: batch_item<R, MOVE, 4>(*sp, bs, id, it.y, st, red, a, t0); break;
+      default: batch_item<R, MOVE, kMaxSpin>(*sp, bs, id, it.y, st, red, a, t0); break;
+    }
     __syncthreads();  // the image and s_item are rewritten by the next item
   }
 }

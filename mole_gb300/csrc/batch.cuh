@@ -95,13 +95,14 @@ __device__ __forceinline__ R div_t(R a, R b) {
   else return __fdividef(a, b);
 }
 
-// Orbital values of spin block `spin` at r (the first kMaxSpin orbitals; the
-// unused ones have zero coefficients) and the e-n Jastrow value.
-template <class R>
-__device__ __forceinline__ void batch_orbitals(const SysParams<R>& sp, int spin, const R (&r)[3], R (&phi)[kMaxSpin],
+// Orbital values of spin block `spin` at r (the first MS orbitals, MS the
+// system's larger spin block; the unused ones have zero coefficients) and the
+// e-n Jastrow value.
+template <class R, int MS>
+__device__ __forceinline__ void batch_orbitals(const SysParams<R>& sp, int spin, const R (&r)[3], R (&phi)[MS],
                                                R& jen) {
 #pragma unroll
-  for (int k = 0; k < kMaxSpin; ++k) phi[k] = 0;
+  for (int k = 0; k < MS; ++k) phi[k] = 0;
   jen = 0;
   for (int I = 0; I < sp.n_nuc; ++I) {
     const R d0 = r[0] - sp.nuc_pos[3 * I], d1 = r[1] - sp.nuc_pos[3 * I + 1], d2 = r[2] - sp.nuc_pos[3 * I + 2];
@@ -121,7 +122,7 @@ __device__ __forceinline__ void batch_orbitals(const SysParams<R>& sp, int spin,
         else chi = (kind == kSto2px ? d0 : (kind == kSto2py ? d1 : d2)) * e;
       }
 #pragma unroll
-      for (int k = 0; k < kMaxSpin; ++k) phi[k] += sp.coef[spin][k][b] * chi;
+      for (int k = 0; k < MS; ++k) phi[k] += sp.coef[spin][k][b] * chi;
     }
     if (sp.en_on) jen += div_t<R>(sp.en_coef[I] * rr, (R)1 + sp.en_a * rr);
   }
@@ -178,7 +179,7 @@ struct BatchWalker {
 // Rebuilds both inverses in FP64 from fresh orbital values by Gauss-Jordan
 // elimination with partial pivoting (the matrix in registers, padded to
 // kMaxSpin x kMaxSpin; the inverse written straight to the shared slots).
-template <class R>
+template <class R, int MS>
 __device__ bool batch_refresh(const SysParams<R>& sp, const BatchWalker<R>& wk) {
   bool ok = true;
   for (int spin = 0; spin < 2; ++spin) {
@@ -187,38 +188,38 @@ __device__ bool batch_refresh(const SysParams<R>& sp, const BatchWalker<R>& wk) 
     const int e0 = spin ? wk.nu : 0;
     double* inv = wk.B(spin);
     const int nt = wk.nt;
-    double a[kMaxSpin][kMaxSpin];
+    double a[MS][MS];
 #pragma unroll
-    for (int i = 0; i < kMaxSpin; ++i) {
+    for (int i = 0; i < MS; ++i) {
       if (i < n) {
         const R r[3] = {wk.xr(e0 + i, 0), wk.xr(e0 + i, 1), wk.xr(e0 + i, 2)};
-        R phi[kMaxSpin], jen;
-        batch_orbitals<R>(sp, spin, r, phi, jen);
+        R phi[MS], jen;
+        batch_orbitals<R, MS>(sp, spin, r, phi, jen);
 #pragma unroll
-        for (int k = 0; k < kMaxSpin; ++k) a[i][k] = up_d<R>(phi[k]);
+        for (int k = 0; k < MS; ++k) a[i][k] = up_d<R>(phi[k]);
       } else {
 #pragma unroll
-        for (int k = 0; k < kMaxSpin; ++k) a[i][k] = 0.0;
+        for (int k = 0; k < MS; ++k) a[i][k] = 0.0;
       }
     }
     for (int i = 0; i < n; ++i)
       for (int j = 0; j < n; ++j) inv[(i * n + j) * nt] = i == j ? 1.0 : 0.0;
 #pragma unroll
-    for (int col = 0; col < kMaxSpin; ++col) {
+    for (int col = 0; col < MS; ++col) {
       if (col >= n) break;
       int piv = col;
       double best = fabs(a[col][col]);
 #pragma unroll
-      for (int r = col + 1; r < kMaxSpin; ++r)
+      for (int r = col + 1; r < MS; ++r)
         if (r < n && fabs(a[r][col]) > best) {
           best = fabs(a[r][col]);
           piv = r;
         }
 #pragma unroll
-      for (int r = col + 1; r < kMaxSpin; ++r)
+      for (int r = col + 1; r < MS; ++r)
         if (r == piv) {
 #pragma unroll
-          for (int j = 0; j < kMaxSpin; ++j) {
+          for (int j = 0; j < MS; ++j) {
             const double t = a[col][j];
             a[col][j] = a[r][j];
             a[r][j] = t;
@@ -233,14 +234,14 @@ __device__ bool batch_refresh(const SysParams<R>& sp, const BatchWalker<R>& wk) 
       ok = ok && (p != 0.0);
       const double ip = 1.0 / p;
 #pragma unroll
-      for (int j = 0; j < kMaxSpin; ++j) a[col][j] *= ip;
+      for (int j = 0; j < MS; ++j) a[col][j] *= ip;
       for (int j = 0; j < n; ++j) inv[(col * n + j) * nt] *= ip;
 #pragma unroll
-      for (int r = 0; r < kMaxSpin; ++r) {
+      for (int r = 0; r < MS; ++r) {
         if (r == col || r >= n) continue;
         const double f = a[r][col];
 #pragma unroll
-        for (int j = 0; j < kMaxSpin; ++j) a[r][j] -= f * a[col][j];
+        for (int j = 0; j < MS; ++j) a[r][j] -= f * a[col][j];
         for (int j = 0; j < n; ++j) inv[(r * n + j) * nt] -= f * inv[(col * n + j) * nt];
       }
     }
@@ -250,7 +251,7 @@ __device__ bool batch_refresh(const SysParams<R>& sp, const BatchWalker<R>& wk) 
 
 // One Metropolis move of electron e (box or Gaussian, the random streams of
 // Walker::move); returns 1 when accepted.
-template <class R, int MOVE>
+template <class R, int MOVE, int MS>
 __device__ __forceinline__ int batch_move(const SysParams<R>& sp, const BatchWalker<R>& wk, int e, R step,
                                           uint64_t seed, uint32_t wid, uint32_t t) {
   const int N = wk.nu + wk.nd;
@@ -307,12 +308,12 @@ __device__ __forceinline__ int batch_move(const SysParams<R>& sp, const BatchWal
       xn[c] = wk.x(e, c);  // global load, consumed only if the move is accepted
     }
   }
-  R phi[kMaxSpin], jn;
-  batch_orbitals<R>(sp, spin, rn, phi, jn);
+  R phi[MS], jn;
+  batch_orbitals<R, MS>(sp, spin, rn, phi, jn);
   const R jo = sp.en_on ? batch_jen<R>(sp, ro) : (R)0;
   double ratio = 0.0;
 #pragma unroll
-  for (int k = 0; k < kMaxSpin; ++k)
+  for (int k = 0; k < MS; ++k)
     if (k < n) ratio += up_d<R>(phi[k]) * B[(k * n + i) * nt];
   R dJ = jn - jo;
   for (int j = 0; j < N; ++j) {
@@ -337,26 +338,26 @@ __device__ __forceinline__ int batch_move(const SysParams<R>& sp, const BatchWal
 #pragma unroll
     for (int c = 0; c < 3; ++c) wk.set_x(e, c, xn[c] + up_d<R>(dx[c]));
   }
-  double v[kMaxSpin], col[kMaxSpin];
+  double v[MS], col[MS];
   double* Bw = wk.B(spin);
 #pragma unroll
-  for (int j = 0; j < kMaxSpin; ++j) {
+  for (int j = 0; j < MS; ++j) {
     if (j >= n) break;
     double s = 0.0;
 #pragma unroll
-    for (int k = 0; k < kMaxSpin; ++k)
+    for (int k = 0; k < MS; ++k)
       if (k < n) s += up_d<R>(phi[k]) * Bw[(k * n + j) * nt];
     v[j] = s - (j == i ? 1.0 : 0.0);
   }
   const double ir = 1.0 / ratio;
 #pragma unroll
-  for (int k = 0; k < kMaxSpin; ++k)
+  for (int k = 0; k < MS; ++k)
     if (k < n) col[k] = Bw[(k * n + i) * nt] * ir;
 #pragma unroll
-  for (int k = 0; k < kMaxSpin; ++k) {
+  for (int k = 0; k < MS; ++k) {
     if (k >= n) break;
 #pragma unroll
-    for (int j = 0; j < kMaxSpin; ++j)
+    for (int j = 0; j < MS; ++j)
       if (j < n) Bw[(k * n + j) * nt] -= col[k] * v[j];
   }
   return 1;
@@ -365,7 +366,7 @@ __device__ __forceinline__ int batch_move(const SysParams<R>& sp, const BatchWal
 // Local energy -1/2 sum_i lap_i psi / psi + V in log-derivative form: orbital
 // gradients and Laplacians in R contracted with the FP64 inverse, Jastrow and
 // potential terms re-evaluated per electron (each pair from both sides).
-template <class R>
+template <class R, int MS>
 __device__ double batch_local_energy(const SysParams<R>& sp, const BatchWalker<R>& wk) {
   const int N = wk.nu + wk.nd;
   const int nt = wk.nt;
@@ -376,11 +377,11 @@ __device__ double batch_local_energy(const SysParams<R>& sp, const BatchWalker<R
     const int i = spin ? e - wk.nu : e;
     const double* B = wk.B(spin);
     const R r[3] = {wk.xr(e, 0), wk.xr(e, 1), wk.xr(e, 2)};
-    OneBody<R, kMaxSpin, 0> o;
-    one_body<R, kMaxSpin, 0, true, false>(sp, spin, r, o);
+    OneBody<R, MS, 0> o;
+    one_body<R, MS, 0, true, false>(sp, spin, r, o);
     double gD[3] = {0.0, 0.0, 0.0}, lD = 0.0;
 #pragma unroll
-    for (int k = 0; k < kMaxSpin; ++k)
+    for (int k = 0; k < MS; ++k)
       if (k < n) {
         const double b = B[(k * n + i) * nt];
         gD[0] += up_d<R>(o.grad[k][0]) * b;
@@ -412,7 +413,10 @@ __device__ double batch_local_energy(const SysParams<R>& sp, const BatchWalker<R
 
 // One work item: walkers [w0, w0 + blockDim.x) of one system, all sweeps of
 // the call; writes the item's kNMom partial sums (deterministic CTA order).
-template <class R, int MOVE>
+// MS = max(nu, nd) bounds the unrolled orbital and inverse loops: a guarded
+// iteration past a spin block's size would still issue its FP64
+// instructions, each holding the FP64 pipe as long as a useful one.
+template <class R, int MOVE, int MS>
 __device__ void batch_item(const SysParams<R>& sp, const BatchSystem& bs, int id, int w0, double* st, double* red,
                            const BatchArgs& a, uint32_t t0) {
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -444,7 +448,7 @@ __device__ void batch_item(const SysParams<R>& sp, const BatchSystem& bs, int id
       if constexpr (F64) wk.X[k * nt] = v;
       else wk.Xr[k * nt] = (R)v;
     }
-    bool ok = batch_refresh<R>(sp, wk);
+    bool ok = batch_refresh<R, MS>(sp, wk);
     const int total = a.n_eq + a.n_steps;
     const int refresh = a.refresh > 0 ? a.refresh : 100;
     const R step = (R)bs.step;
@@ -452,10 +456,10 @@ __device__ void batch_item(const SysParams<R>& sp, const BatchSystem& bs, int id
     int naccept = 0;
     for (int it = 0; it < total; ++it) {
       const uint32_t t = t0 + (uint32_t)it;
-      for (int e = 0; e < N; ++e) naccept += batch_move<R, MOVE>(sp, wk, e, step, bs.seed, (uint32_t)w, t);
-      if ((it + 1) % refresh == 0) ok = batch_refresh<R>(sp, wk) && ok;
+      for (int e = 0; e < N; ++e) naccept += batch_move<R, MOVE, MS>(sp, wk, e, step, bs.seed, (uint32_t)w, t);
+      if ((it + 1) % refresh == 0) ok = batch_refresh<R, MS>(sp, wk) && ok;
       if (it < a.n_eq) continue;
-      const double E = batch_local_energy<R>(sp, wk);
+      const double E = batch_local_energy<R, MS>(sp, wk);
       sE += E;
       sE2 += E * E;
       bsum += E;
