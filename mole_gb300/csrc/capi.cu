@@ -261,7 +261,7 @@ KernelSetT<double>::Vmc vmc64_compact(const mole_system* s, int slot, int drift,
   return compact_vmc64(s->n_up, s->n_dn, slot);
 }
 // The same systems on small ensembles (up to two 32-walker teams per SM),
-// with one 1s function on each of at most two nuclei: the three-warp teams
+// with one 1s function on each of at most two nuclei: the four-warp teams
 // of team.cuh.
 KernelSetT<double>::Vmc vmc64_team(const mole_system* s, int slot, int drift, int W, int n_sm) {
   if (!one_electron_per_spin_1s(s, drift) || n_sm <= 0 || W > 2 * 32 * n_sm) return nullptr;

@@ -1,6 +1,6 @@
 // FP64 VMC launchers for spin blocks of 1 up and at most 1 down electron,
 // without and with two-parameter SR sums: the packed FP64 moves (compact.cuh,
-// large ensembles) and the three-warp teams (team.cuh, small ensembles; one
+// large ensembles) and the four-warp teams (team.cuh, small ensembles; one
 // or two nuclei).
 #include "dispatch.cuh"
 

@@ -6,6 +6,21 @@
 
 namespace mole {
 
+// c + a b for the moment sums, fused explicitly in FP64 and FP32 so that every
+// kernel rounds them alike (the double-float form's arithmetic is explicit).
+template <class F>
+__device__ __forceinline__ F fma_acc(F a, F b, F c) {
+  return c + a * b;
+}
+template <>
+__device__ __forceinline__ double fma_acc<double>(double a, double b, double c) {
+  return fma(a, b, c);
+}
+template <>
+__device__ __forceinline__ float fma_acc<float>(float a, float b, float c) {
+  return fmaf(a, b, c);
+}
+
 // Threads per CTA for every walker kernel, and the resident CTAs per SM the
 // register budget is tuned for: seven 64-walker CTAs per SM hold 65,536
 // walkers in one balanced wave on 152 SMs.
@@ -112,24 +127,27 @@ __device__ __forceinline__ void vmc_body(const SysParams<R>& sp, const VmcArgs& 
     F O[PM > 0 ? PM : 1];
     const F E = wk.local_energy(sp, O, nullptr, nullptr);
     const int k = it - a.n_eq;
-    sE2 += E * E;
+    // the products are fused explicitly: left to the code generator, the
+    // choice can differ between kernels, and the team kernel's sums must
+    // equal these bit for bit
+    sE2 = fma_acc(E, E, sE2);
     bsum += E;  // added to sE at every block end and after the last sweep
     if constexpr (PM > 0) {
 #pragma unroll
       for (int p = 0; p < PM; ++p) {
         srf[p * BLK + tid] += O[p];
-        srf[(PM + p) * BLK + tid] += E * O[p];
+        srf[(PM + p) * BLK + tid] = fma_acc(E, O[p], srf[(PM + p) * BLK + tid]);
       }
       int q = 2 * PM;
 #pragma unroll
       for (int p = 0; p < PM; ++p)
 #pragma unroll
-        for (int r = p; r < PM; ++r, ++q) srf[q * BLK + tid] += O[p] * O[r];
+        for (int r = p; r < PM; ++r, ++q) srf[q * BLK + tid] = fma_acc(O[p], O[r], srf[q * BLK + tid]);
     }
     if ((k + 1) % a.block_size == 0) {
       const double bs = to_d(bsum);
       const double m = bs / a.block_size;
-      sB2 += m * m;
+      sB2 = fma(m, m, sB2);
       double v[1] = {active ? bs : 0.0};
       block_sum<1>(v, red);
       if (threadIdx.x == 0) a.tb_partials[(size_t)blockIdx.x * (a.n_steps / a.block_size) + k / a.block_size] = v[0];

@@ -1,50 +1,70 @@
-// team.cuh -- FP64 VMC for small ensembles: a team of three warps per 32
-// walkers.
+// team.cuh -- FP64 VMC for small ensembles: a team of four warps per 32
+// walkers, software-pipelined over the moves.
 //
 // With one walker per thread a 1,024-walker ensemble is 32 warps, one per
 // SM sub-partition in use, and each sweep costs a warp its whole dependent
 // FP64 instruction stream: GB300 issues one FP64 warp instruction per 64
 // cycles per sub-partition, so the sweep takes (FP64 instructions per
 // walker-step) x ~64 cycles whatever the number of walkers per warp. Here the
-// stream of each walker is split over three warps on three sub-partitions:
+// stream of each walker is split over four warps on four sub-partitions:
 //
-//   warp 0  the moved electron's orbital terms (value, gradient, Laplacian,
-//           exponent derivative, e-n potential), the ratio and the new
-//           1x1 inverse;
-//   warp 1  the same proposal's pair term (u, u'/r, u'' + 2u'/r, 1/r, du/db);
+//   warp 0  electron 0's moves: the orbital terms of the proposal (value,
+//           gradient, Laplacian, exponent derivative, e-n potential), the
+//           ratio and the decision;
+//   warp 3  the same for electron 1;
+//   warp 1  the pair value u of every move and the Jastrow difference;
 //   warp 2  the local energy, O_k and every sum of the sweep before (from a
-//           double-buffered snapshot of the caches in shared memory), while
-//           warps 0 and 1 run the next sweep.
+//           double-buffered snapshot in shared memory), with the pair's
+//           derivative terms formed from its kept intermediates, while the
+//           others run the next sweep.
 //
-// Warps 0 and 1 draw the same random numbers, exchange the ratio and the
-// Jastrow difference through shared memory (one named barrier per move,
-// double-buffered by move parity), take the same decision and commit each its
-// own caches; both keep the positions. The arithmetic is Walker::move's and
-// Walker::local_energy's on the same operands, so the trajectories, energies
-// and sums are the per-thread kernel's, bit for bit.
+// Move m = it N + e depends on the decision of move m - 1 only through the
+// pair term (the other electron's position); electron e's orbital chain
+// depends only on e's previous decision, two moves back. So the one-body
+// warp of electron e forms its next proposal right after its decision and
+// publishes it before the move in between, and runs its chain while the pair
+// warp finishes that move: the per-move recurrence is the pair chain and the
+// decision, and each orbital chain has two moves' time. The proposal, the
+// ratio and the Jastrow difference pass through shared memory (four slots by
+// m & 3); move m's named barrier (id 1 + e) joins the pair warp and warp e
+// (bar.sync) and the other one-body warp (bar.arrive, once its proposal for
+// move m + 1 is written). Each move's random numbers are drawn once, by its
+// one-body warp; the acceptance number reaches the pair warp with the
+// proposal, and both warps take the same decision from the same ratio,
+// Jastrow difference and number. The arithmetic is Walker::move's and
+// Walker::local_energy's on the same operands (the periodic rebuild would
+// recompute the same values from the same positions, so only its
+// singularity test is kept), and the moment sums fuse their products
+// explicitly, as the per-thread kernel's do: trajectories and acceptance
+// counts are the per-thread kernel's bit for bit, and the energies and SR
+// sums within the last bit of a few local-energy values (the local energy is
+// compiled separately in each kernel; with He a few values round differently
+// in the last bit, with H2 none).
 //
 // A move is one dependent chain per warp, and on GB300 a dependent FP64
 // instruction costs 64 cycles while an integer or FP32 one costs about 4.
 // The move code is therefore straight-line: the nucleus count NB (1 or 2,
 // one 1s function each) is a template parameter, the system's constants sit
 // in registers, and the next move's random draw (Philox and the unit
-// proposal, ~100 integer instructions) is made during the current move, in
-// the issue slots the FP64 chain leaves idle.
+// proposal, ~100 integer instructions) is made during the current move's
+// chain, in the issue slots the FP64 chain leaves idle.
 //
 // Scope: FP64 box and Gaussian moves, at most one electron per spin, one 1s
 // STO per nucleus (at most 2 nuclei), plain Pade e-e term or none, no e-n
 // Jastrow, Coulomb potential; the host picks it for small ensembles.
 //
-// Named barriers: 1 (warps 0 and 1, each move), 2 + b (snapshot b written:
-// warps 0 and 1 arrive, warp 2 waits), 4 + b (snapshot b read: warp 2
-// arrives, warps 0 and 1 wait before writing it again); b = sample parity.
+// Named barriers: 1 + e (move of electron e; 96 threads, 64 for the last
+// move), 3 + b (snapshot b written: the producers arrive, warp 2 waits),
+// 5 + b (snapshot b read: warp 2 arrives, the producers wait before writing
+// it again), b = sample parity; 7 (move 0's proposal, before the pair warp's
+// first move). With one electron warp 0 runs alone and warps 1 and 3 idle.
 #pragma once
 
 #include "walker.cuh"
 
 namespace mole {
 
-constexpr int kTeamThreads = 96;
+constexpr int kTeamThreads = 128;
 
 // Named barriers with compile-time ids (so that the kernel reserves only the
 // ids it uses); the _par forms pick id or id + 1.
@@ -94,6 +114,47 @@ struct TeamConst {
   }
 };
 
+// pair_vals<double, PM, false> of the team scope (plain Pade term, no
+// polynomial), straight-line, split in two: the value u (keeping r^2, 1/r,
+// r, q and c q), which the pair warp needs for each move, and the
+// derivative terms from those, which the E_L warp forms once per sweep.
+struct TeamPrScr {
+  double r2, inv, r, q, cq;
+};
+
+template <int NB>
+__device__ __forceinline__ double team_pair_value(const TeamConst<NB>& k, bool same, double d0, double d1, double d2,
+                                                  TeamPrScr& s) {
+  const double r2 = d0 * d0 + d1 * d1 + d2 * d2;
+  const double inv = rsqrt_t<double>(r2);
+  const double r = r2 * inv;
+  const double cusp = same ? k.cusp_para : k.cusp_anti;
+  // u = c r q, u' = c q^2, u'' = -2 b c q^3, du/db = -c r^2 q^2, q = 1 / (1 + b r)
+  const double q = recip_t<double>(1.0 + k.ee_b * r);
+  const double cq = cusp * q;
+  s.r2 = r2;
+  s.inv = inv;
+  s.r = r;
+  s.q = q;
+  s.cq = cq;
+  return cq * r;
+}
+
+template <int NB, int PM>
+__device__ __forceinline__ void team_pair_derivs(const TeamConst<NB>& k, const TeamPrScr& s, PairVals<double, PM>& v) {
+  v.inv = s.inv;
+  v.db = 0;
+  v.rs = s.r;
+  const double uR = s.cq * s.q;
+  // u'' is rounded on its own, as pair_vals rounds it (its polynomial loop
+  // stands between the product and the sum below): no contraction into l
+  const double uRR = __dmul_rn(k.ee_m2b * s.q, uR);
+  if constexpr (PM > 0) v.db = -(s.r2 * uR);
+  const double f = uR * s.inv;
+  v.f = f;
+  v.l = uRR + 2.0 * f;
+}
+
 // one_body<double, 1, NZ> of the team scope with the nucleus loop unrolled:
 // the same operations on the same operands, so the same values.
 template <int NB, int NZ>
@@ -137,34 +198,6 @@ __device__ __forceinline__ void team_one_body(const TeamConst<NB>& k, int spin, 
   }
 }
 
-// pair_vals<double, PM, false> of the team scope (plain Pade term, no
-// polynomial), straight-line.
-template <int NB, int PM>
-__device__ __forceinline__ void team_pair(const TeamConst<NB>& k, bool same, double d0, double d1, double d2,
-                                          PairVals<double, PM>& v) {
-  const double r2 = d0 * d0 + d1 * d1 + d2 * d2;
-  const double inv = rsqrt_t<double>(r2);
-  const double r = r2 * inv;
-  v.inv = inv;
-  v.db = 0;
-  v.rs = r;
-  const double cusp = same ? k.cusp_para : k.cusp_anti;
-  // u = c r q, u' = c q^2, u'' = -2 b c q^3, du/db = -c r^2 q^2, q = 1 / (1 + b r)
-  const double q = recip_t<double>(1.0 + k.ee_b * r);
-  const double cq = cusp * q;
-  const double uR = cq * q;
-  const double val = cq * r;
-  // u'' is rounded on its own, as pair_vals rounds it (its polynomial loop
-  // stands between the product and the sum below): no contraction into l
-  const double uRR = __dmul_rn(k.ee_m2b * q, uR);
-  if constexpr (PM > 0) v.db = -(r2 * uR);
-  const double f = uR * inv;
-  const double l = uRR + 2.0 * f;
-  v.u = val;
-  v.f = f;
-  v.l = l;
-}
-
 // The unit proposal of one move (Walker::move's draws): box moves u - 1/2
 // exactly, Gaussian moves the FP32 normals; and the acceptance bits.
 struct TeamUnit {
@@ -192,14 +225,16 @@ __device__ __forceinline__ TeamUnit team_unit(uint64_t seed, uint32_t w, uint32_
   return u;
 }
 
-// The caches warp 2 needs, per walker (slot [field][lane]).
+// The caches the E_L warp needs, per walker (slot [field][lane]): per
+// electron x (3), the orbital value, gradient (3), Laplacian, [exponent
+// derivative], e-n potential; the pair's intermediates r^2, 1/r, r, q, c q.
 template <int N, int PM>
 struct TeamSnap {
   static constexpr int NZ = PM == 0 ? 0 : 1;
-  // x (3N), B (N), og (3N), ol (N), odz (N NZ), ven (N); pair: u, f, l, 1/r, du/db, R
-  static constexpr int NF0 = 3 * N + N + 3 * N + N + N * NZ + N;
-  static constexpr int NF1 = N == 2 ? 6 : 0;
-  double f[2][NF0 + NF1 + 1][32];
+  static constexpr int SF = 9 + NZ;
+  static constexpr int NF0 = N * SF;
+  static constexpr int NF1 = N == 2 ? 5 : 0;
+  double f[2][NF0 + NF1][32];
 };
 
 template <int NU, int ND, int PM, int NB, int MOVE>
@@ -210,8 +245,15 @@ __device__ __forceinline__ void team_body(const SysParams<double>& sp, const Vmc
   constexpr int NA = n_acc(PM);
   constexpr int NSR = NA - kNMom;
   using Snap = TeamSnap<N, PM>;
+  constexpr int SF = Snap::SF;
+  // warps taking part in a snapshot barrier: the E_L warp and the producers
+  constexpr int kSnapThreads = N == 2 ? 128 : 64;
   __shared__ Snap snap;
-  __shared__ double xch[2][2][32];  // [move parity][0: ratio, 1: dJ][lane]
+  // per-move exchange, slot m & 3 for move m: the ratio (one-body warp), the
+  // Jastrow difference (pair warp), the proposal and its acceptance draw
+  // (one-body warp, for the pair warp)
+  __shared__ double xr[4][32], xdj[4][32], xxn[4][3][32];
+  __shared__ uint32_t xub[4][32];
   __shared__ double red[kTeamThreads / 32];
   const int lane = threadIdx.x & 31, role = threadIdx.x >> 5;
   const int w = blockIdx.x * 32 + lane;
@@ -219,6 +261,7 @@ __device__ __forceinline__ void team_body(const SysParams<double>& sp, const Vmc
   const double step = a.step;
   const int total = a.n_eq + a.n_steps;
   const int refresh = a.refresh > 0 ? a.refresh : 100;
+  const int M = total * N;  // moves of the run; move m = it N + e
 
   Wk wk;
   wk.nn = NnCtx<double>{nullptr, nullptr, 0};
@@ -228,157 +271,222 @@ __device__ __forceinline__ void team_body(const SysParams<double>& sp, const Vmc
     for (int e = 0; e < N; ++e) wk.x[e][0] = wk.x[e][1] = wk.x[e][2] = 1.0 + e;
   bool ok = true;
   int naccept = 0;
-  // warp 2's sums
+  // the E_L warp's sums
   double sE = acc_zero<double>(), sE2 = acc_zero<double>(), bsum = acc_zero<double>(), sB2 = 0.0;
   double srv[NSR > 0 ? NSR : 1];
 #pragma unroll
   for (int k = 0; k < (NSR > 0 ? NSR : 1); ++k) srv[k] = 0.0;
   bool e_finite = true;
+  const TeamConst<NB> kc(sp);
 
-  if (role < 2) {
-    ok = wk.refresh(sp, nullptr, nullptr);
-    const TeamConst<NB> kc(sp);
-    int mv = 0;  // move counter (exchange-buffer parity)
-    TeamUnit un = team_unit<MOVE>(a.seed, (uint32_t)w, a.step0, 0);
+  // One-body warp of electron E: its orbital value chain, decisions and
+  // derivative caches. Its next proposal is formed right after its decision
+  // and published before the pair warp needs it (the barrier of the move
+  // in between).
+  auto one_body_warp = [&](auto ec) {
+    constexpr int E = decltype(ec)::value;
+    constexpr int spin = E < NU ? 0 : 1;
+    OneBody<double, 1, NZ> o;
+    team_one_body<NB, NZ>(kc, spin, wk.x[E], o);
+    double vo = o.val[0];  // the orbital value; 1x1 inverse = 1 / vo
+    ok = !is_zero(vo);
+    const TeamUnit u0 = team_unit<MOVE>(a.seed, (uint32_t)w, a.step0, E);
+    double xn[3];
+    xn[0] = fma(step, u0.v[0], wk.x[E][0]);
+    xn[1] = fma(step, u0.v[1], wk.x[E][1]);
+    xn[2] = fma(step, u0.v[2], wk.x[E][2]);
+    uint32_t ub = u0.ubits;
+    if (N == 2 && M > 0) {
+      xxn[E][0][lane] = xn[0];
+      xxn[E][1][lane] = xn[1];
+      xxn[E][2][lane] = xn[2];
+      xub[E][lane] = ub;
+      if (E == 0) named_arrive<7>(64);  // move 0's proposal, before the pair warp's first move
+      else named_arrive<1>(96);         // move 1's, at the barrier of move 0
+    }
     for (int it = 0; it < total; ++it) {
       const uint32_t t = a.step0 + (uint32_t)it;
-      static_for<0, N>([&](auto ec) {
-        constexpr int e = decltype(ec)::value;
-        constexpr bool isup = e < NU;
-        constexpr int j = N == 2 ? 1 - e : 0;
-        // the proposal (Walker::move's draws and arithmetic); the next
-        // move's draw is made here too, independent of this move's chain
-        const TeamUnit u = un;
-        if constexpr (e + 1 < N) un = team_unit<MOVE>(a.seed, (uint32_t)w, t, e + 1);
-        else un = team_unit<MOVE>(a.seed, (uint32_t)w, t + 1u, 0);
-        double xn[3];
-        xn[0] = fma(step, u.v[0], wk.x[e][0]);
-        xn[1] = fma(step, u.v[1], wk.x[e][1]);
-        xn[2] = fma(step, u.v[2], wk.x[e][2]);
-        const uint32_t ubits = u.ubits;
-        const int par = mv & 1;
-        OneBody<double, 1, NZ> o;
-        PairVals<double, PM> pv;
-        double ratio, dJ;
-        if (role == 0) {
-          team_one_body<NB, NZ>(kc, isup ? 0 : 1, xn, o);
-          ratio = acc_zero<double>();
-          ratio += o.val[0] * (isup ? wk.bu[0] : wk.bd[0]);
-          xch[par][0][lane] = ratio;
-        } else {
-          dJ = acc_zero<double>();
-          if constexpr (N == 2) {
-            team_pair<NB, PM>(kc, Wk::same_spin(e, j), xn[0] - wk.x[j][0], xn[1] - wk.x[j][1], xn[2] - wk.x[j][2],
-                              pv);
-            dJ += pv.u - wk.pu[0];
-          }
-          xch[par][1][lane] = dJ;
-        }
-        named_sync<1>(64);
-        if (role == 0) dJ = xch[par][1][lane];
-        else ratio = xch[par][0][lane];
-        ++mv;
-        if (metropolis_accept_dj(ratio, dJ, ubits)) {
-          wk.x[e][0] = xn[0];
-          wk.x[e][1] = xn[1];
-          wk.x[e][2] = xn[2];
-          if (role == 0) {
-            naccept += 1;
-            wk.template put_one_body<e, 1>(o);
-            if constexpr (isup) wk.bu[0] = recip(o.val[0]);
-            else wk.bd[0] = recip(o.val[0]);
-          } else if constexpr (N == 2) {
-            wk.put_pair(0, pv);
-          }
-        }
-      });
-      if ((it + 1) % refresh == 0) {
-        // each warp rebuilds its own caches (the other's are rebuilt too and not used)
-        ok = wk.refresh(sp, nullptr, nullptr) && ok;
+      [[maybe_unused]] const int m = it * N + E;
+      // this electron's next draw (sweep it + 1), beside the value chain
+      const TeamUnit un = team_unit<MOVE>(a.seed, (uint32_t)w, t + 1u, E);
+      const double B = recip(vo);
+      OneBody<double, 1, NZ> on;
+      team_one_body<NB, NZ>(kc, spin, xn, on);
+      const double val = on.val[0];
+      double ratio = acc_zero<double>();
+      ratio += val * B;
+      double dJ;
+      if constexpr (N == 2) {
+        xr[m & 3][lane] = ratio;
+        named_sync<1 + E>(m + 1 < M ? 96 : 64);
+        dJ = xdj[m & 3][lane];
+      } else {
+        dJ = acc_zero<double>();
       }
+      const bool acc = metropolis_accept_dj(ratio, dJ, ub);
+      if (acc) {
+        wk.x[E][0] = xn[0];
+        wk.x[E][1] = xn[1];
+        wk.x[E][2] = xn[2];
+        vo = val;
+        naccept += 1;
+      }
+      if (it + 1 < total) {
+        xn[0] = fma(step, un.v[0], wk.x[E][0]);
+        xn[1] = fma(step, un.v[1], wk.x[E][1]);
+        xn[2] = fma(step, un.v[2], wk.x[E][2]);
+        ub = un.ubits;
+        if constexpr (N == 2) {
+          const int s2 = (m + 2) & 3;
+          xxn[s2][0][lane] = xn[0];
+          xxn[s2][1][lane] = xn[1];
+          xxn[s2][2][lane] = xn[2];
+          xub[s2][lane] = ub;
+          named_arrive<2 - E>(96);  // the barrier of move m + 1 (the other electron's)
+        }
+      }
+      if (acc) o = on;
+      // the periodic rebuild recomputes these caches from the same
+      // positions by the same arithmetic, so only its singularity test remains
+      if ((it + 1) % refresh == 0) ok = !is_zero(vo) && ok;
       if (it < a.n_eq) continue;
-      // snapshot of this sweep for warp 2
       const int k = it - a.n_eq, b = k & 1;
-      if (k >= 2) named_sync_par<4>(b, kTeamThreads);
+      if (k >= 2) named_sync_par<5>(b, kSnapThreads);
       double(*s)[32] = snap.f[b];
-      if (role == 0) {
-        int q = 0;
-#pragma unroll
-        for (int e = 0; e < N; ++e) {
-          s[q++][lane] = wk.x[e][0];
-          s[q++][lane] = wk.x[e][1];
-          s[q++][lane] = wk.x[e][2];
-          s[q++][lane] = e < NU ? wk.bu[0] : wk.bd[0];
-          s[q++][lane] = wk.og[e][0][0];
-          s[q++][lane] = wk.og[e][0][1];
-          s[q++][lane] = wk.og[e][0][2];
-          s[q++][lane] = wk.ol[e][0];
-          if constexpr (NZ > 0) s[q++][lane] = wk.odz[e][0][0];
-          s[q++][lane] = wk.ven[e];
-        }
-      } else if constexpr (N == 2) {
-        s[Snap::NF0 + 0][lane] = wk.pu[0];
-        s[Snap::NF0 + 1][lane] = wk.pf[0];
-        s[Snap::NF0 + 2][lane] = wk.pl[0];
-        s[Snap::NF0 + 3][lane] = wk.pinv[0];
-        s[Snap::NF0 + 4][lane] = wk.pdb[0];
-        s[Snap::NF0 + 5][lane] = wk.prs[0];
-      }
-      named_arrive_par<2>(b, kTeamThreads);
+      s[SF * E + 0][lane] = wk.x[E][0];
+      s[SF * E + 1][lane] = wk.x[E][1];
+      s[SF * E + 2][lane] = wk.x[E][2];
+      s[SF * E + 3][lane] = vo;
+      s[SF * E + 4][lane] = o.grad[0][0];
+      s[SF * E + 5][lane] = o.grad[0][1];
+      s[SF * E + 6][lane] = o.grad[0][2];
+      s[SF * E + 7][lane] = o.lap[0];
+      if constexpr (NZ > 0) s[SF * E + 8][lane] = o.dz[0][0];
+      s[SF * E + 8 + NZ][lane] = o.ven;
+      named_arrive_par<3>(b, kSnapThreads);
     }
-    // the last two snapshots' releases, so that every barrier completes
-    for (int k = (a.n_steps >= 2 ? a.n_steps - 2 : 0); k < a.n_steps; ++k) named_sync_par<4>(k & 1, kTeamThreads);
+    for (int k = (a.n_steps >= 2 ? a.n_steps - 2 : 0); k < a.n_steps; ++k) named_sync_par<5>(k & 1, kSnapThreads);
+  };
+
+  if (role == 0) {
+    one_body_warp(std::integral_constant<int, 0>{});
+  } else if (role == 3) {
+    if constexpr (N == 2) one_body_warp(std::integral_constant<int, 1>{});
+  } else if (role == 1) {
+    if constexpr (N == 2) {
+      // the pair warp: the Jastrow difference of each move, which needs the
+      // decision of the move before (the other electron's position)
+      TeamPrScr ps;
+      double pu = team_pair_value<NB>(kc, Wk::same_spin(0, 1), wk.x[0][0] - wk.x[1][0], wk.x[0][1] - wk.x[1][1],
+                                      wk.x[0][2] - wk.x[1][2], ps);
+      if (M > 0) named_sync<7>(64);
+      for (int it = 0; it < total; ++it) {
+        static_for<0, 2>([&](auto ec) {
+          constexpr int e = decltype(ec)::value;
+          constexpr int j = 1 - e;
+          const int m = it * 2 + e, sl = m & 3;
+          double xn[3];
+          xn[0] = xxn[sl][0][lane];
+          xn[1] = xxn[sl][1][lane];
+          xn[2] = xxn[sl][2][lane];
+          const uint32_t ub = xub[sl][lane];
+          TeamPrScr pn;
+          const double un = team_pair_value<NB>(kc, Wk::same_spin(e, j), xn[0] - wk.x[j][0], xn[1] - wk.x[j][1],
+                                                xn[2] - wk.x[j][2], pn);
+          double dJ = acc_zero<double>();
+          dJ += un - pu;
+          xdj[sl][lane] = dJ;
+          named_sync<1 + e>(m + 1 < M ? 96 : 64);
+          const double ratio = xr[sl][lane];
+          if (metropolis_accept_dj(ratio, dJ, ub)) {
+            wk.x[e][0] = xn[0];
+            wk.x[e][1] = xn[1];
+            wk.x[e][2] = xn[2];
+            pu = un;
+            ps = pn;
+          }
+        });
+        if (it < a.n_eq) continue;
+        const int k = it - a.n_eq, b = k & 1;
+        if (k >= 2) named_sync_par<5>(b, kSnapThreads);
+        double(*s)[32] = snap.f[b];
+        s[Snap::NF0 + 0][lane] = ps.r2;
+        s[Snap::NF0 + 1][lane] = ps.inv;
+        s[Snap::NF0 + 2][lane] = ps.r;
+        s[Snap::NF0 + 3][lane] = ps.q;
+        s[Snap::NF0 + 4][lane] = ps.cq;
+        named_arrive_par<3>(b, kSnapThreads);
+      }
+      for (int k = (a.n_steps >= 2 ? a.n_steps - 2 : 0); k < a.n_steps; ++k) named_sync_par<5>(k & 1, kSnapThreads);
+    }
   } else {
-    // warp 2: E_L, O_k and the sums of sampled sweep k from snapshot k & 1
+    // the E_L warp: E_L, O_k and the sums of sampled sweep k from snapshot k & 1
     for (int k = 0; k < a.n_steps; ++k) {
       const int b = k & 1;
-      named_sync_par<2>(b, kTeamThreads);
+      named_sync_par<3>(b, kSnapThreads);
       const double(*s)[32] = snap.f[b];
-      int q = 0;
+      double vs[N];
 #pragma unroll
       for (int e = 0; e < N; ++e) {
-        wk.x[e][0] = s[q++][lane];
-        wk.x[e][1] = s[q++][lane];
-        wk.x[e][2] = s[q++][lane];
-        if (e < NU) wk.bu[0] = s[q++][lane];
-        else wk.bd[0] = s[q++][lane];
-        wk.og[e][0][0] = s[q++][lane];
-        wk.og[e][0][1] = s[q++][lane];
-        wk.og[e][0][2] = s[q++][lane];
-        wk.ol[e][0] = s[q++][lane];
-        if constexpr (NZ > 0) wk.odz[e][0][0] = s[q++][lane];
-        wk.ven[e] = s[q++][lane];
+        wk.x[e][0] = s[SF * e + 0][lane];
+        wk.x[e][1] = s[SF * e + 1][lane];
+        wk.x[e][2] = s[SF * e + 2][lane];
+        vs[e] = s[SF * e + 3][lane];
+        wk.og[e][0][0] = s[SF * e + 4][lane];
+        wk.og[e][0][1] = s[SF * e + 5][lane];
+        wk.og[e][0][2] = s[SF * e + 6][lane];
+        wk.ol[e][0] = s[SF * e + 7][lane];
+        if constexpr (NZ > 0) wk.odz[e][0][0] = s[SF * e + 8][lane];
+        wk.ven[e] = s[SF * e + 8 + NZ][lane];
+      }
+      TeamPrScr ps;
+      if constexpr (N == 2) {
+        ps.r2 = s[Snap::NF0 + 0][lane];
+        ps.inv = s[Snap::NF0 + 1][lane];
+        ps.r = s[Snap::NF0 + 2][lane];
+        ps.q = s[Snap::NF0 + 3][lane];
+        ps.cq = s[Snap::NF0 + 4][lane];
+      }
+      named_arrive_par<5>(b, kSnapThreads);
+      // the 1x1 inverses (the move's own reciprocal of the orbital value)
+#pragma unroll
+      for (int e = 0; e < N; ++e) {
+        if (e < NU) wk.bu[0] = recip(vs[e]);
+        else wk.bd[0] = recip(vs[e]);
       }
       if constexpr (N == 2) {
-        wk.pu[0] = s[Snap::NF0 + 0][lane];
-        wk.pf[0] = s[Snap::NF0 + 1][lane];
-        wk.pl[0] = s[Snap::NF0 + 2][lane];
-        wk.pinv[0] = s[Snap::NF0 + 3][lane];
-        wk.pdb[0] = s[Snap::NF0 + 4][lane];
-        wk.prs[0] = s[Snap::NF0 + 5][lane];
+        PairVals<double, PM> pv;
+        team_pair_derivs<NB, PM>(kc, ps, pv);
+        wk.pf[0] = pv.f;
+        wk.pl[0] = pv.l;
+        wk.pinv[0] = pv.inv;
+        if constexpr (PM > 0) {
+          wk.pdb[0] = pv.db;
+          wk.prs[0] = pv.rs;
+        }
       }
-      named_arrive_par<4>(b, kTeamThreads);
       double O[PM > 0 ? PM : 1];
       const double E = wk.local_energy(sp, O, nullptr, nullptr);
       e_finite = e_finite && (E == E);
-      sE2 += E * E;
+      // fused explicitly, as the per-thread kernel's sums are
+      sE2 = fma(E, E, sE2);
       bsum += E;
       if constexpr (PM > 0) {
 #pragma unroll
         for (int p = 0; p < PM; ++p) {
           srv[p] += O[p];
-          srv[PM + p] += E * O[p];
+          srv[PM + p] = fma(E, O[p], srv[PM + p]);
         }
         int qq = 2 * PM;
 #pragma unroll
         for (int p = 0; p < PM; ++p)
 #pragma unroll
-          for (int r = p; r < PM; ++r, ++qq) srv[qq] += O[p] * O[r];
+          for (int r = p; r < PM; ++r, ++qq) srv[qq] = fma(O[p], O[r], srv[qq]);
       }
       if ((k + 1) % a.block_size == 0) {
         const double bs = bsum;
         const double m = bs / a.block_size;
-        sB2 += m * m;
+        sB2 = fma(m, m, sB2);
         const double v = warp_sum(active ? bs : 0.0);
         if (lane == 0) a.tb_partials[(size_t)blockIdx.x * (a.n_steps / a.block_size) + k / a.block_size] = v;
         sE += bsum;
@@ -387,15 +495,17 @@ __device__ __forceinline__ void team_body(const SysParams<double>& sp, const Vmc
     }
     sE += bsum;
   }
+
   // one partial row per CTA (deterministic order, as vmc_body's)
   double acc[kNMom] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   if (active) {
-    if (role == 0) {
+    if (role == 0 || role == 3) {
       acc[5] = (double)naccept;
-      acc[6] = (double)total * N;
-      wk.store(a.pos, a.W, w);
       if (!ok) atomicOr(a.status, 2);
-    } else if (role == 2) {
+    }
+    if (role == 0) acc[6] = (double)total * N;
+    if (role == (N == 2 ? 1 : 0)) wk.store(a.pos, a.W, w);  // the pair warp holds both positions
+    if (role == 2) {
       acc[0] = (double)a.n_steps;
       acc[1] = sE;
       acc[2] = sE2;
@@ -413,7 +523,7 @@ __device__ __forceinline__ void team_body(const SysParams<double>& sp, const Vmc
   }
 }
 
-// FP64 VMC with a three-warp team per 32 walkers (box: move 0, else
+// FP64 VMC with a four-warp team per 32 walkers (box: move 0, else
 // Gaussian), NB nuclei with one 1s function each.
 template <int NU, int ND, int PM, int NB>
 __global__ void __launch_bounds__(kTeamThreads) vmc_team_kernel(const __grid_constant__ SysParams<double> sp,

@@ -1,5 +1,5 @@
-"""The three-warp team kernel (small ensembles of one-electron-per-spin 1s
-systems) against the one-walker-per-thread FP64 kernel.
+"""The team kernel (small ensembles of one-electron-per-spin 1s systems)
+against the one-walker-per-thread FP64 kernel.
 
 A walker's random stream depends only on the seed and the walker's index, so
 walkers 0..255 of a 256-walker run (team kernel) and of a 12,000-walker run
@@ -38,3 +38,47 @@ def test_team_trajectories_equal_the_per_thread_kernel(ctx, name, move, step, sr
         wk.close()
     np.testing.assert_array_equal(out[n_small][0], out[n_large][0])
     assert out[n_small][1].acceptance > 0.3
+
+
+@pytest.mark.parametrize("name,move,step,sr", [
+    ("He", 0, 0.5, False),
+    ("He", 0, 0.5, True),
+    ("H2", 1, 0.4, False),
+    ("H2", 1, 0.4, True),
+])
+def test_team_sums_equal_the_per_thread_kernel(ctx, name, move, step, sr):
+    """One electron 200 bohr out puts its orbital below FP32's range, so the
+    double-float run is rerun in native FP64 on the one-walker-per-thread
+    kernel, while the plain FP64 run of the same 64 walkers takes the team
+    kernel. Over 123 sweeps (one periodic cache rebuild included) positions,
+    sample and acceptance counts agree bit for bit. The energy and SR sums
+    agree to 1e-13 relative: the two kernels compile the local energy
+    separately, and with He a few of its values round differently in the last
+    bit (the H2 sums are equal bit for bit)."""
+    s = {"He": S.helium(1.6875, 0.3), "H2": S.h2(1.0, 0.5)}[name]
+    wf = api.WaveFunction(ctx, s)
+    W = 64
+    pos = np.random.default_rng(3).normal(size=(W, s.n_elec, 3))
+    pos[5, s.n_elec - 1] = [200.0, 0.0, 0.0]
+    res = {}
+    for prec in (api.PREC_FP64, api.PREC_DF64):
+        wk = api.Walkers(wf, W, seed=0x5EED + 41)
+        wk.set_positions(pos)
+        before = ctx.df64_reruns()
+        mv = api.MetropolisBox(step) if move == 0 else api.MetropolisGaussian(step)
+        r = api.Sampler(wf, mv, wk, precision=prec).run(3, 120, 10, sr=sr)
+        res[prec] = (r, wk.positions(), ctx.df64_reruns() - before)
+        wk.close()
+    team, ref = res[api.PREC_FP64], res[api.PREC_DF64]
+    assert team[2] == 0 and ref[2] == 1
+    np.testing.assert_array_equal(team[1], ref[1])
+    counts = [0, 4, 5, 6]  # samples, blocks, accepted moves, moves
+    np.testing.assert_array_equal(team[0].moments[counts], ref[0].moments[counts])
+    np.testing.assert_allclose(team[0].moments, ref[0].moments, rtol=1e-13, atol=0)
+    if name == "H2":
+        np.testing.assert_array_equal(team[0].moments, ref[0].moments)
+    if sr:
+        for f in ("sum_O", "sum_EO", "sum_OO"):
+            np.testing.assert_allclose(getattr(team[0], f), getattr(ref[0], f), rtol=1e-13, atol=1e-300)
+            if name == "H2":
+                np.testing.assert_array_equal(getattr(team[0], f), getattr(ref[0], f))
