@@ -243,10 +243,10 @@ int mole_vmc_run(mole_walkers* w, const mole_vmc_opts* opts, double* moments, do
  * working memory is one fixed 2 MiB device array that every GPU loading the
  * library holds until the process exits; the call is rejected with
  * MOLE_ERR_SHAPE when (CTAs of the launch) x (accumulators + time blocks) does not
- * fit it. The first call on a device looks up that array's device address,
- * so make it before any stream capture; the address is kept for the life of
- * the process and stays valid while the device's primary context lives (a
- * cudaDeviceReset by the caller invalidates it). Every call shares the array:
+ * fit it. The first call on a device looks up that array's device address;
+ * the address is kept for the life of the process and stays valid while the
+ * device's primary context lives (a cudaDeviceReset by the caller invalidates
+ * it). Every call shares the array:
  * calls that overlap on the GPU (other streams, other threads) race. The call
  * reads its status word back and synchronises `stream` (a cudaStream_t of the
  * system's device, NULL for the default stream; a stream of another device is
