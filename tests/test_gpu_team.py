@@ -7,7 +7,7 @@ walkers 0..255 of a 256-walker run (team kernel) and of a 12,000-walker run
 kernel) started from the same positions follow the same trajectory. The team
 kernel computes the same operations on the same operands, so the positions
 must agree bit for bit, with one nucleus (He) and two (H2), with and without
-the SR sums."""
+the SR sums, and with one electron (H, where one warp runs the moves)."""
 import numpy as np
 import pytest
 
@@ -17,14 +17,19 @@ from mole_gb300 import system as S
 pytestmark = pytest.mark.gpu
 
 
+SYSTEMS = {"He": lambda: S.helium(1.6875, 0.3), "H2": lambda: S.h2(1.0, 0.5),
+           "H": lambda: S.hydrogen_sto(0.8)}
+
+
 @pytest.mark.parametrize("name,move,step,sr", [
     ("He", 0, 0.5, False),
     ("He", 0, 0.5, True),
     ("H2", 1, 0.4, False),
     ("H2", 1, 0.4, True),
+    ("H", 0, 1.0, False),
 ])
 def test_team_trajectories_equal_the_per_thread_kernel(ctx, name, move, step, sr):
-    s = {"He": S.helium(1.6875, 0.3), "H2": S.h2(1.0, 0.5)}[name]
+    s = SYSTEMS[name]()
     wf = api.WaveFunction(ctx, s)
     n_small, n_large = 256, 12000
     pos = np.random.default_rng(11).normal(size=(n_large, s.n_elec, 3))
@@ -45,6 +50,7 @@ def test_team_trajectories_equal_the_per_thread_kernel(ctx, name, move, step, sr
     ("He", 0, 0.5, True),
     ("H2", 1, 0.4, False),
     ("H2", 1, 0.4, True),
+    ("H", 0, 1.0, False),
 ])
 def test_team_sums_equal_the_per_thread_kernel(ctx, name, move, step, sr):
     """One electron 200 bohr out puts its orbital below FP32's range, so the
@@ -54,8 +60,8 @@ def test_team_sums_equal_the_per_thread_kernel(ctx, name, move, step, sr):
     sample and acceptance counts agree bit for bit. The energy and SR sums
     agree to 1e-13 relative: the two kernels compile the local energy
     separately, and with He a few of its values round differently in the last
-    bit (the H2 sums are equal bit for bit)."""
-    s = {"He": S.helium(1.6875, 0.3), "H2": S.h2(1.0, 0.5)}[name]
+    bit (the H2 and H sums are equal bit for bit)."""
+    s = SYSTEMS[name]()
     wf = api.WaveFunction(ctx, s)
     W = 64
     pos = np.random.default_rng(3).normal(size=(W, s.n_elec, 3))
@@ -75,10 +81,10 @@ def test_team_sums_equal_the_per_thread_kernel(ctx, name, move, step, sr):
     counts = [0, 4, 5, 6]  # samples, blocks, accepted moves, moves
     np.testing.assert_array_equal(team[0].moments[counts], ref[0].moments[counts])
     np.testing.assert_allclose(team[0].moments, ref[0].moments, rtol=1e-13, atol=0)
-    if name == "H2":
+    if name != "He":
         np.testing.assert_array_equal(team[0].moments, ref[0].moments)
     if sr:
         for f in ("sum_O", "sum_EO", "sum_OO"):
             np.testing.assert_allclose(getattr(team[0], f), getattr(ref[0], f), rtol=1e-13, atol=1e-300)
-            if name == "H2":
+            if name != "He":
                 np.testing.assert_array_equal(getattr(team[0], f), getattr(ref[0], f))
