@@ -36,10 +36,10 @@
 // recompute the same values from the same positions, so only its
 // singularity test is kept), and the moment sums fuse their products
 // explicitly, as the per-thread kernel's do: trajectories and acceptance
-// counts are the per-thread kernel's bit for bit, and the energies and SR
-// sums within the last bit of a few local-energy values (the local energy is
-// compiled separately in each kernel; with He a few values round differently
-// in the last bit, with H2 none).
+// counts are the per-thread kernel's bit for bit, and so are the energies and
+// SR sums for H2 and H; with He a few local-energy values differ in the last
+// bit (not caused by the periodic rebuild, the walker's distance or the
+// split of the value and derivative terms; not otherwise explained).
 //
 // A move is one dependent chain per warp, and on GB300 a dependent FP64
 // instruction costs 64 cycles while an integer or FP32 one costs about 4.

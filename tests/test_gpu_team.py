@@ -58,9 +58,9 @@ def test_team_sums_equal_the_per_thread_kernel(ctx, name, move, step, sr):
     kernel, while the plain FP64 run of the same 64 walkers takes the team
     kernel. Over 123 sweeps (one periodic cache rebuild included) positions,
     sample and acceptance counts agree bit for bit. The energy and SR sums
-    agree to 1e-13 relative: the two kernels compile the local energy
-    separately, and with He a few of its values round differently in the last
-    bit (the H2 and H sums are equal bit for bit)."""
+    are equal bit for bit for H2 and H; with He a few local-energy values
+    differ in the last bit (cause not identified), so they are held to
+    1e-13 relative."""
     s = SYSTEMS[name]()
     wf = api.WaveFunction(ctx, s)
     W = 64
